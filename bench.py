@@ -1,0 +1,320 @@
+"""Benchmark of the shallow-water step on the conformal cubed sphere (GB300).
+
+Workload (one "step" = one RK4 time step): C384 (6 x 384 x 384 interior cells,
+halo 3) from the seeded state with orography (spherical harmonics, h = 8000 m +
+200 m RMS perturbation, 40 m/s non-divergent wind, orography clipped to
+0-2000 m), CFL 0.5.  Metric: interior cell-steps per second of the mixed
+FP32/FP64 lane; the FP64 parity lane is measured beside it on the same state.
+
+  value      device-timed throughput, inputs resident in HBM, L2 flushed between
+             timed steps (CUDA events on the library's own stream)
+  e2e        the same metric through the C ABI with host buffers: every step is
+             ccs_set_state (pinned host -> device) + ccs_step(1) + ccs_get_state
+             (device -> pinned host)
+  roofline   the mixed stage kernel's average launch duration against the
+             measured HBM copy bandwidth
+  cpu_baseline  the CPU FP64 oracle (a restatement of the reference step) on the
+             host cores, on a bounded sample of the workload
+
+--impl reference times only the reference CPU step (the oracle) on the same
+workload and prints its own line.  Under torchrun (N > 1) every rank advances
+its own C384 replica (the single-member step does not shard): value is the
+total over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+N_BENCH = 384
+HALO = 3
+SEED = 1
+# Algorithmic bytes per interior cell-step (RK4, four stages): mixed lane 396 B
+# (FP32 state and accumulator, FP64 metric streamed), FP64 lane 600 B.
+ALG_BYTES_MIXED = 396.0
+ALG_BYTES_FP64 = 600.0
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def __enter__(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.rows.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = []
+        for k, n in enumerate(names):
+            if any(len(r) > 5 + k and r[5 + k].lower() == "active" for r in self.rows):
+                reasons.append(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_launch(name: str):
+    """dram bytes per launch from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / "roofline_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(name)
+    except Exception:
+        return None
+
+
+def build_case(N=N_BENCH, seed=SEED, oro=True):
+    from conformal_cubed_sphere_gb300 import _lib as L
+    from conformal_cubed_sphere_gb300 import model as M
+    mesh = M.Mesh(N, HALO)
+    s = M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=seed, lmax_oro=8 if oro else 0)
+    dt = M.cfl_dt(mesh, s, 0.5)
+    return mesh, s, dt
+
+
+def time_device_steps(stepper, torch, steps: int, flush: "torch.Tensor"):
+    """Per-step CUDA-event timing on the library's stream, L2 flushed in between."""
+    st = torch.cuda.ExternalStream(stepper.stream_ptr)
+    total = 0.0
+    for _ in range(steps):
+        with torch.cuda.stream(st):
+            flush.add_(1.0)  # writes > L2 bytes
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(st)
+        stepper.step_async(1)
+        ev1.record(st)
+        ev1.synchronize()
+        total += ev0.elapsed_time(ev1)
+    return total / 1e3  # seconds
+
+
+def kernel_launch_avg_ms(stepper, steps: int):
+    stepper.timing(enable=1, reset=1)
+    stepper.step(steps)
+    ms, n = stepper.timing(enable=0, reset=1)
+    return ms / max(n, 1), n
+
+
+def e2e_rate(stepper, mesh, state, steps: int, torch):
+    """ccs_set_state + ccs_step(1) + ccs_get_state per step, pinned host buffers."""
+    from conformal_cubed_sphere_gb300 import model as M
+    pin_in = {k: torch.from_numpy(state[k].copy()).pin_memory() for k in M.STATE_FIELDS}
+    pin_out = {k: torch.empty(mesh.ncell, dtype=torch.float64).pin_memory() for k in M.STATE_FIELDS}
+    sin = M.State({k: v.numpy() for k, v in pin_in.items()})
+    sout = M.State({k: v.numpy() for k, v in pin_out.items()})
+    # inputs the lane uploads / outputs it downloads
+    lane_mixed = stepper._cfg.precision == 1
+    n_in = 3 if lane_mixed else 8
+    n_out = 8
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        stepper.set_state(sin)
+        stepper.step(1)
+        stepper.get_state(sout)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    cells = 6 * mesh.N * mesh.N
+    nb = mesh.ncell * 8
+    return cells * steps / dt, n_in * nb, n_out * nb
+
+
+def cpu_baseline(mesh, state, dt, steps=1):
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    orc = O.Oracle.from_mesh(mesh, threads=threads)
+    orc.set_state(state.arrays)
+    orc.run(dt, 1)  # warm-up (first touch of the work arrays)
+    t0 = time.perf_counter()
+    orc.run(dt, steps)
+    el = time.perf_counter() - t0
+    cells = 6 * mesh.N * mesh.N
+    return {"value": cells * steps / el, "unit": "cell-steps/s", "cores": O.lib().orc_get_threads(),
+            "kind": "port",
+            "sample": f"{steps} RK4 step(s) of C{mesh.N} FP64 (CPU restatement of the reference step), "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    mesh, s, dt = build_case()
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    orc = O.Oracle.from_mesh(mesh, threads=threads)
+    orc.set_state(s.arrays)
+    steps = max(1, min(args.steps, 3))
+    warm = max(1, min(args.warmup, 1))
+    orc.run(dt, warm)
+    t0 = time.perf_counter()
+    orc.run(dt, steps)
+    el = time.perf_counter() - t0
+    cells = 6 * mesh.N * mesh.N
+    v = cells * steps / el
+    line = {
+        "impl": "reference", "metric": "C384 cell-steps/s", "value": v, "unit": "cell-steps/s",
+        "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "C384 seeded state with orography, RK4, CFL 0.5", "N": mesh.N, "halo": HALO},
+        "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": O.lib().orc_get_threads(), "kind": "port",
+                         "sample": f"{steps} RK4 steps of C384 after {warm} warm-up step(s)"},
+        "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--N", type=int, default=N_BENCH)
+    ap.add_argument("--fp64-steps", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = _dist()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from conformal_cubed_sphere_gb300 import model as M
+
+    mesh, s, dt = build_case(args.N)
+    cells = 6 * mesh.N * mesh.N
+    phibar = 8000.0 * mesh.gravity
+    mixed = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
+    mixed.set_state(s)
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+    mixed.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    barrier()
+    with sampler:
+        t_mixed = time_device_steps(mixed, torch, args.steps, flush)
+    barrier()
+    if ws > 1:
+        t = torch.tensor([t_mixed], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_mixed = float(t.item())
+    value = ws * cells * args.steps / t_mixed
+
+    # roofline of the dominant kernel (the mixed stage kernel)
+    avg_ms, nl = kernel_launch_avg_ms(mixed, 4)
+    hbm, peak_kind = _peaks()
+    bytes_per_launch = ALG_BYTES_MIXED / 4.0 * cells
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
+    traffic = _traffic_per_launch(f"mixed_stage_C{mesh.N}")
+
+    # FP64 parity lane on the same state
+    f64 = M.Stepper(mesh, dt, precision="fp64", device=local)
+    f64.set_state(s)
+    f64.step(1)
+    torch.cuda.synchronize()
+    t_f64 = time_device_steps(f64, torch, args.fp64_steps, flush)
+    fp64_value = cells * args.fp64_steps / t_f64
+    avg64_ms, _ = kernel_launch_avg_ms(f64, 1)
+
+    # end to end through the C ABI
+    e2e_steps = max(3, min(20, args.steps))
+    mixed2 = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
+    mixed2.set_state(s)
+    e2e, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
+
+    if rank != 0:
+        return
+    cpu = None if args.no_cpu else cpu_baseline(mesh, s, dt, steps=1)
+    line = {
+        "metric": "C384 cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_mixed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 metric transforms)",
+        "data": "synthetic (seeded spherical harmonics)",
+        "config": {"workload": f"C{mesh.N} seeded state with orography, RK4, CFL 0.5, mixed FP32/FP64 lane",
+                   "N": mesh.N, "halo": HALO, "dt_s": dt, "l2": "flushed (256 MB write) between timed steps",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "fp64_lane": {"value": fp64_value, "unit": "cell-steps/s", "ms_per_step": 1e3 * t_f64 / args.fp64_steps,
+                      "kernel_ms_avg": avg64_ms, "mixed_over_fp64": value / ws / fp64_value},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "kernel": "mixed_stage_kernel", "kernel_ms_avg": avg_ms,
+                     "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind},
+        "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 4 * args.steps,
+        "clocks": sampler.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,84 @@
+"""Builds the in-tree CUDA library ``_build/libccs_gpu.so`` for sm_103a.
+
+Every translation unit is compiled in parallel with nvcc and linked into one
+shared library with the CUDA runtime linked statically.  Host code is compiled
+with ``-ffp-contract=off``: the FP64 set-up arithmetic (metric products, halo
+transforms) must not be fused on aarch64 hosts, where gcc contracts by default.
+The FP64 parity kernels are compiled with ``-fmad=false`` for the same reason.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = BUILD / "libccs_gpu.so"
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+# (source, extra flags)
+UNITS = [
+    ("ccs_fp64.cu", ["-fmad=false"]),
+    ("ccs_mixed.cu", []),
+    ("ccs_api.cu", []),
+    ("ccs_host.cpp", []),
+]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found; the CUDA library cannot be built")
+    return cand
+
+
+def _common(nvcc: str) -> list[str]:
+    return [
+        nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+        "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", f"-I{CSRC}", f"-I{PKG.parent / 'include'}",
+    ]
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    """Compile and link; returns the library path.  Skips work when up to date."""
+    BUILD.mkdir(exist_ok=True)
+    srcs = [CSRC / s for s, _ in UNITS]
+    deps = srcs + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "ccs_gpu.h", Path(__file__)]
+    if not force and LIB.exists():
+        t = LIB.stat().st_mtime
+        if all(d.stat().st_mtime <= t for d in deps):
+            return LIB
+    nvcc = _nvcc()
+    common = _common(nvcc)
+
+    def compile_one(unit):
+        src, extra = unit
+        obj = BUILD / (Path(src).stem + ".o")
+        cmd = common + extra + ["-c", str(CSRC / src), "-o", str(obj)]
+        if src.endswith(".cpp"):
+            cmd = common + extra + ["-x", "c++", "-c", str(CSRC / src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout, r.stderr, file=sys.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, UNITS))
+    tmp = BUILD / "libccs_gpu.so.tmp"
+    cmd = [nvcc, ARCH, "-shared", "-cudart", "static", "-o", str(tmp)] + [str(o) for o in objs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="--force" in sys.argv))

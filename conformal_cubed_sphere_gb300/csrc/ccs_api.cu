@@ -1,0 +1,1043 @@
+// ccs_api.cu -- the C ABI (include/ccs_gpu.h): handles, device buffers, stage
+// descriptors, CUDA-graph capture of a step, state transfer and diagnostics.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ccs_internal.h"
+#include "ccs_kernels.h"
+
+using namespace ccs;
+
+namespace {
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+#define CCS_TRY(h, call)                                                       \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      if (h) (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_);    \
+      return CCS_ERR_CUDA;                                                     \
+    }                                                                          \
+  } while (0)
+
+// Device copy of one grid's metric, shared by every member on that grid.
+struct DeviceMesh {
+  int device = 0;
+  Layout L{};
+  double *buf64 = nullptr;  // FP64 lane arrays
+  int32_t *push = nullptr;
+  MeshF64 m64{};
+  float *buf32 = nullptr;   // mixed lane arrays
+  double *xf = nullptr;     // mixed lane FP64 halo transforms
+  MeshMixed mm{};
+  double radius = 0.;
+  ~DeviceMesh() {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(device);
+    if (buf64) cudaFree(buf64);
+    if (push) cudaFree(push);
+    if (buf32) cudaFree(buf32);
+    if (xf) cudaFree(xf);
+    cudaSetDevice(cur);
+  }
+};
+
+}  // namespace
+
+struct MixedLane;
+
+struct ccs_handle {
+  ccs_config cfg{};
+  std::shared_ptr<DeviceMesh> mesh;
+  Layout L{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // FP64 lane buffers
+  double *sbuf = nullptr;
+  StateF64 S[3]{};
+  double *zonal = nullptr, *merid = nullptr;
+  double *acc[3]{}, *tend[3]{};
+  // stage descriptors: RK stages, final stage with sphere winds, tendency-only
+  std::vector<F64Stage> h_stages;
+  F64Stage *d_stages = nullptr;
+  int n_rk = 0;  // number of RK stages (4 or 3)
+  WorkItem *d_work = nullptr;
+  int nwork = 0;
+  int grid = 0;
+  bool sphere_valid = false;
+  cudaGraphExec_t g_step = nullptr, g_step_sw = nullptr;
+  // timing
+  bool timing = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double kernel_ms = 0.;
+  int64_t launches = 0;
+  // diagnostics
+  double *d_partials = nullptr;
+  // mixed lane
+  struct MixedLane *mixed = nullptr;
+};
+
+static const int kDiagBlocks = 512;
+
+static int upload_field(ccs_handle *h, double *dst, const double *src) {
+  const Layout &L = h->L;
+  CCS_TRY(h, cudaMemcpy2DAsync(dst, (size_t)L.pitch * sizeof(double), src, (size_t)L.nh * sizeof(double),
+                               (size_t)L.nh * sizeof(double), (size_t)L.nh * 6, cudaMemcpyHostToDevice,
+                               h->stream));
+  return CCS_OK;
+}
+
+static int download_field(ccs_handle *h, double *dst, const double *src) {
+  const Layout &L = h->L;
+  CCS_TRY(h, cudaMemcpy2DAsync(dst, (size_t)L.nh * sizeof(double), src, (size_t)L.pitch * sizeof(double),
+                               (size_t)L.nh * sizeof(double), (size_t)L.nh * 6, cudaMemcpyDeviceToHost,
+                               h->stream));
+  return CCS_OK;
+}
+
+static int validate_config(const ccs_config *c) {
+  if (!c) return CCS_ERR_ARG;
+  if (c->N < 1 || c->N > 8192 || c->halo < 3 || c->halo > c->N) return CCS_ERR_ARG;
+  if (c->scheme != CCS_RK4 && c->scheme != CCS_RK3_TVD) return CCS_ERR_ARG;
+  if (c->precision != CCS_FP64 && c->precision != CCS_MIXED) return CCS_ERR_ARG;
+  if (c->e_dissipation != CCS_EDISS_ZERO && c->e_dissipation != CCS_EDISS_RECONSTRUCT) return CCS_ERR_ARG;
+  if (!(c->dx > 0.) || !(c->dy > 0.) || !(c->dt > 0.) || !(c->radius > 0.) || !(c->gravity > 0.))
+    return CCS_ERR_ARG;
+  if (!std::isfinite(c->dx) || !std::isfinite(c->dy) || !std::isfinite(c->dt) || !std::isfinite(c->omega))
+    return CCS_ERR_ARG;
+  return CCS_OK;
+}
+
+// matmul of two 2x2 column-major matrices as gfortran inlines it (c = 0; c += ...)
+static void matmul22(const double *X, const double *Y, double *M) {
+  for (int c = 0; c < 2; c++)
+    for (int r = 0; r < 2; r++) {
+      double s = 0.;
+      for (int k = 0; k < 2; k++) s = s + X[r + 2 * k] * Y[k + 2 * c];
+      M[r + 2 * c] = s;
+    }
+}
+
+static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *mv);
+static int mixed_handle_create(ccs_handle *h);
+static void mixed_handle_destroy(ccs_handle *h);
+static int mixed_set_state(ccs_handle *h, const ccs_state_view *s);
+static int mixed_get_state(ccs_handle *h, ccs_state_view *s);
+static int mixed_step(ccs_handle *h, int nsteps, bool sync);
+static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv);
+static int mixed_diag(ccs_handle *h, double *mass, double *energy);
+
+static int build_mesh(ccs_handle *h, const ccs_mesh_view *mv) {
+  auto dm = std::make_shared<DeviceMesh>();
+  dm->device = h->cfg.device;
+  dm->L = h->L;
+  dm->radius = h->cfg.radius;
+  const Layout &L = h->L;
+  const size_t nref = (size_t)L.nh * L.nh * 6;
+  const size_t nf = (size_t)L.field;
+  // 15 FP64 arrays: sqrtG phis f ig11 ig12 ig21 ig22 aig11..22 gia11..22
+  CCS_TRY(h, cudaMalloc(&dm->buf64, 15 * nf * sizeof(double)));
+  CCS_TRY(h, cudaMemsetAsync(dm->buf64, 0, 15 * nf * sizeof(double), h->stream));
+  std::vector<double> tmp(15 * nref, 0.);
+  double *t[15];
+  for (int k = 0; k < 15; k++) t[k] = tmp.data() + k * nref;
+  for (size_t c = 0; c < nref; c++) {
+    t[0][c] = mv->sqrtG[c];
+    t[1][c] = mv->phis[c];
+    t[2][c] = mv->f[c];
+    const double *IG = &mv->matrixIG[4 * c];
+    t[3][c] = IG[0];  // IG(1,1)
+    t[4][c] = IG[2];  // IG(1,2)
+    t[5][c] = IG[1];  // IG(2,1)
+    t[6][c] = IG[3];  // IG(2,2)
+    double M[4];
+    matmul22(&mv->matrixA[4 * c], IG, M);  // projection_mod.F90:90
+    t[7][c] = M[0]; t[8][c] = M[2]; t[9][c] = M[1]; t[10][c] = M[3];
+    matmul22(&mv->matrixG[4 * c], &mv->matrixIA[4 * c], M);  // projection_mod.F90:71
+    t[11][c] = M[0]; t[12][c] = M[2]; t[13][c] = M[1]; t[14][c] = M[3];
+  }
+  for (int k = 0; k < 15; k++) {
+    int rc = upload_field(h, dm->buf64 + k * nf, t[k]);
+    if (rc) return rc;
+  }
+  double *b = dm->buf64;
+  dm->m64.sqrtG = b + 0 * nf; dm->m64.phis = b + 1 * nf; dm->m64.f = b + 2 * nf;
+  dm->m64.ig11 = b + 3 * nf; dm->m64.ig12 = b + 4 * nf; dm->m64.ig21 = b + 5 * nf; dm->m64.ig22 = b + 6 * nf;
+  dm->m64.aig11 = b + 7 * nf; dm->m64.aig12 = b + 8 * nf; dm->m64.aig21 = b + 9 * nf; dm->m64.aig22 = b + 10 * nf;
+  dm->m64.gia11 = b + 11 * nf; dm->m64.gia12 = b + 12 * nf; dm->m64.gia21 = b + 13 * nf; dm->m64.gia22 = b + 14 * nf;
+  std::vector<int32_t> push;
+  if (!build_push_table(L, push)) {
+    h->err = "ghost tables are inconsistent";
+    return CCS_ERR_MESH;
+  }
+  CCS_TRY(h, cudaMalloc(&dm->push, push.size() * sizeof(int32_t)));
+  CCS_TRY(h, cudaMemcpyAsync(dm->push, push.data(), push.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                             h->stream));
+  dm->m64.push = dm->push;
+  if (h->cfg.precision == CCS_MIXED) {
+    int rc = mixed_mesh_setup(h, dm.get(), mv);
+    if (rc) return rc;
+  }
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  h->mesh = dm;
+  return CCS_OK;
+}
+
+static int build_f64_lane(ccs_handle *h) {
+  const Layout &L = h->L;
+  const size_t nf = (size_t)L.field;
+  // 3 slots x 6 fields + zonal + merid + acc(3) + tend(3) = 26 fields
+  CCS_TRY(h, cudaMalloc(&h->sbuf, 26 * nf * sizeof(double)));
+  CCS_TRY(h, cudaMemsetAsync(h->sbuf, 0, 26 * nf * sizeof(double), h->stream));
+  double *b = h->sbuf;
+  for (int s = 0; s < 3; s++) {
+    h->S[s].phiG = b; b += nf;
+    h->S[s].u = b; b += nf;
+    h->S[s].v = b; b += nf;
+    h->S[s].phi = b; b += nf;
+    h->S[s].uC = b; b += nf;
+    h->S[s].vC = b; b += nf;
+  }
+  h->zonal = b; b += nf;
+  h->merid = b; b += nf;
+  for (int k = 0; k < 3; k++) { h->acc[k] = b; b += nf; }
+  for (int k = 0; k < 3; k++) { h->tend[k] = b; b += nf; }
+
+  const ccs_config &c = h->cfg;
+  F64Stage base{};
+  base.L = L;
+  base.m = h->mesh->m64;
+  base.y0phiG = h->S[0].phiG; base.y0u = h->S[0].u; base.y0v = h->S[0].v;
+  base.accphiG = h->acc[0]; base.accu = h->acc[1]; base.accv = h->acc[2];
+  base.dx = c.dx; base.dy = c.dy;
+  base.dx60 = 60. * c.dx; base.dy60 = 60. * c.dy;
+  base.ediss = c.e_dissipation;
+  auto mk = [&](int kind, int in, int out, double c1) {
+    F64Stage s = base;
+    s.kind = kind;
+    s.in = h->S[in];
+    s.out = h->S[out];
+    s.c1 = c1;
+    return s;
+  };
+  h->h_stages.clear();
+  const double dt = c.dt;
+  if (c.scheme == CCS_RK4) {
+    h->n_rk = 4;
+    h->h_stages.push_back(mk(K_RK4_1, 0, 1, 0.5 * dt));
+    h->h_stages.push_back(mk(K_RK4_2, 1, 2, 0.5 * dt));
+    h->h_stages.push_back(mk(K_RK4_2, 2, 1, dt));
+    h->h_stages.push_back(mk(K_RK4_4, 1, 0, dt));
+  } else {
+    h->n_rk = 3;
+    h->h_stages.push_back(mk(K_RK3_1, 0, 1, dt));
+    h->h_stages.push_back(mk(K_RK3_2, 1, 2, 0.25 * dt));
+    h->h_stages.push_back(mk(K_RK3_3, 2, 0, 2. / 3. * dt));
+  }
+  F64Stage sw = h->h_stages.back();
+  sw.zonal = h->zonal;
+  sw.merid = h->merid;
+  h->h_stages.push_back(sw);  // final stage with sphere winds
+  F64Stage td = mk(K_TEND, 0, 0, 0.);
+  td.tphiG = h->tend[0]; td.tu = h->tend[1]; td.tv = h->tend[2];
+  h->h_stages.push_back(td);
+  CCS_TRY(h, cudaMalloc(&h->d_stages, h->h_stages.size() * sizeof(F64Stage)));
+  CCS_TRY(h, cudaMemcpyAsync(h->d_stages, h->h_stages.data(), h->h_stages.size() * sizeof(F64Stage),
+                             cudaMemcpyHostToDevice, h->stream));
+  // work list: all tiles of the six panels
+  const int ntx = (L.N + F64_TX - 1) / F64_TX, nty = (L.N + F64_TY - 1) / F64_TY;
+  std::vector<WorkItem> work;
+  for (int p = 0; p < 6; p++)
+    for (int ty = 0; ty < nty; ty++)
+      for (int tx = 0; tx < ntx; tx++) work.push_back(WorkItem{0, (int16_t)p, (int16_t)tx, (int16_t)ty});
+  h->nwork = (int)work.size();
+  CCS_TRY(h, cudaMalloc(&h->d_work, work.size() * sizeof(WorkItem)));
+  CCS_TRY(h, cudaMemcpyAsync(h->d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                             h->stream));
+  h->grid = f64_max_grid(c.device, 1);
+  CCS_TRY(h, cudaMalloc(&h->d_partials, 2 * kDiagBlocks * sizeof(double)));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+// enqueue one step; with_sw: the final stage also writes the sphere winds
+static int f64_enqueue_step(ccs_handle *h, bool with_sw) {
+  for (int k = 0; k < h->n_rk; k++) {
+    const F64Stage *d = h->d_stages + ((k == h->n_rk - 1 && with_sw) ? h->n_rk : k);
+    if (h->timing) CCS_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    CCS_TRY(h, launch_f64_stage(d, h->d_work, h->nwork, h->grid, h->stream));
+    if (h->timing) {
+      CCS_TRY(h, cudaEventRecord(h->ev1, h->stream));
+      CCS_TRY(h, cudaEventSynchronize(h->ev1));
+      float ms = 0.f;
+      CCS_TRY(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+      h->kernel_ms += ms;
+      h->launches++;
+    }
+  }
+  return CCS_OK;
+}
+
+static int f64_capture(ccs_handle *h, bool with_sw, cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  CCS_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const bool t = h->timing;
+  h->timing = false;
+  int rc = f64_enqueue_step(h, with_sw);
+  h->timing = t;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) {
+    h->err = std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e);
+    return CCS_ERR_CUDA;
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    h->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
+    return CCS_ERR_CUDA;
+  }
+  return CCS_OK;
+}
+
+static int f64_step(ccs_handle *h, int nsteps, bool sync) {
+  if (nsteps <= 0) return CCS_OK;
+  if (h->timing) {
+    for (int s = 0; s < nsteps; s++) {
+      int rc = f64_enqueue_step(h, s == nsteps - 1);
+      if (rc) return rc;
+    }
+  } else {
+    if (!h->g_step) {
+      int rc = f64_capture(h, false, &h->g_step);
+      if (rc) return rc;
+      rc = f64_capture(h, true, &h->g_step_sw);
+      if (rc) return rc;
+    }
+    for (int s = 0; s < nsteps - 1; s++) CCS_TRY(h, cudaGraphLaunch(h->g_step, h->stream));
+    CCS_TRY(h, cudaGraphLaunch(h->g_step_sw, h->stream));
+  }
+  h->sphere_valid = true;
+  if (sync) CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int ccs_abi_version(void) { return CCS_ABI_VERSION; }
+
+void *ccs_stream(ccs_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+const char *ccs_strerror(int status) {
+  switch (status) {
+    case CCS_OK: return "ok";
+    case CCS_ERR_ARG: return "invalid argument";
+    case CCS_ERR_CUDA: return "CUDA error";
+    case CCS_ERR_NAN: return "non-finite or non-positive state";
+    case CCS_ERR_TIMEOUT: return "device wait timed out";
+    case CCS_ERR_UNSUPPORTED: return "unsupported option";
+    case CCS_ERR_MESH: return "singular or inconsistent mesh";
+    case CCS_ERR_NOMEM: return "out of memory";
+    case CCS_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char *ccs_last_error(const ccs_handle *h) { return h ? h->err.c_str() : ""; }
+
+static int init_common(const ccs_config *cfg, ccs_handle **out, ccs_handle **hp) {
+  if (!out) return CCS_ERR_ARG;
+  *out = nullptr;
+  int rc = validate_config(cfg);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CCS_ERR_NODEVICE;
+  if (cfg->device < 0 || cfg->device >= ndev) return CCS_ERR_ARG;
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return CCS_ERR_CUDA;
+  ccs_handle *h = new ccs_handle();
+  h->cfg = *cfg;
+  const int nh = cfg->N + 2 * cfg->halo;
+  h->L = make_layout(cfg->N, cfg->halo, round_up(nh, 4));
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return CCS_ERR_CUDA;
+  }
+  cudaEventCreate(&h->ev0);
+  cudaEventCreate(&h->ev1);
+  *hp = h;
+  return CCS_OK;
+}
+
+static int finish_init(ccs_handle *h) {
+  if (h->cfg.precision == CCS_FP64) return build_f64_lane(h);
+  return mixed_handle_create(h);
+}
+
+int ccs_init(const ccs_config *cfg, const ccs_mesh_view *mesh, ccs_handle **out) {
+  if (!mesh || !mesh->sqrtG || !mesh->matrixG || !mesh->matrixIG || !mesh->matrixA || !mesh->matrixIA ||
+      !mesh->f || !mesh->phis)
+    return CCS_ERR_ARG;
+  ccs_handle *h = nullptr;
+  int rc = init_common(cfg, out, &h);
+  if (rc) return rc;
+  rc = build_mesh(h, mesh);
+  if (!rc) rc = finish_init(h);
+  if (rc) {
+    fprintf(stderr, "ccs_init: %s (%s)\n", ccs_strerror(rc), h->err.c_str());
+    ccs_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return CCS_OK;
+}
+
+int ccs_init_shared(const ccs_config *cfg, ccs_handle *owner, ccs_handle **out) {
+  if (!owner || !cfg) return CCS_ERR_ARG;
+  const ccs_config &o = owner->cfg;
+  if (cfg->N != o.N || cfg->halo != o.halo || cfg->dx != o.dx || cfg->dy != o.dy || cfg->device != o.device ||
+      cfg->precision != o.precision || cfg->radius != o.radius)
+    return CCS_ERR_ARG;
+  ccs_handle *h = nullptr;
+  int rc = init_common(cfg, out, &h);
+  if (rc) return rc;
+  h->mesh = owner->mesh;
+  rc = finish_init(h);
+  if (rc) {
+    ccs_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return CCS_OK;
+}
+
+void ccs_destroy(ccs_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  if (h->g_step_sw) cudaGraphExecDestroy(h->g_step_sw);
+  if (h->sbuf) cudaFree(h->sbuf);
+  if (h->d_stages) cudaFree(h->d_stages);
+  if (h->d_work) cudaFree(h->d_work);
+  if (h->d_partials) cudaFree(h->d_partials);
+  if (h->mixed) mixed_handle_destroy(h);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  h->mesh.reset();
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int ccs_set_state(ccs_handle *h, const ccs_state_view *s) {
+  if (!h || !s || !s->phiG || !s->u || !s->v || !s->phi || !s->uC || !s->vC) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (h->cfg.precision == CCS_MIXED) return mixed_set_state(h, s);
+  const double *src[6] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC};
+  double *dst[6] = {h->S[0].phiG, h->S[0].u, h->S[0].v, h->S[0].phi, h->S[0].uC, h->S[0].vC};
+  for (int k = 0; k < 6; k++) {
+    int rc = upload_field(h, dst[k], src[k]);
+    if (rc) return rc;
+  }
+  h->sphere_valid = false;
+  if (s->zonal_wind && s->meridional_wind) {
+    int rc = upload_field(h, h->zonal, s->zonal_wind);
+    if (!rc) rc = upload_field(h, h->merid, s->meridional_wind);
+    if (rc) return rc;
+    h->sphere_valid = true;
+  }
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+int ccs_get_state(ccs_handle *h, ccs_state_view *s) {
+  if (!h || !s) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (h->cfg.precision == CCS_MIXED) return mixed_get_state(h, s);
+  double *dst[6] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC};
+  const double *src[6] = {h->S[0].phiG, h->S[0].u, h->S[0].v, h->S[0].phi, h->S[0].uC, h->S[0].vC};
+  for (int k = 0; k < 6; k++)
+    if (dst[k]) {
+      int rc = download_field(h, dst[k], src[k]);
+      if (rc) return rc;
+    }
+  if (h->sphere_valid) {
+    if (s->zonal_wind) {
+      int rc = download_field(h, s->zonal_wind, h->zonal);
+      if (rc) return rc;
+    }
+    if (s->meridional_wind) {
+      int rc = download_field(h, s->meridional_wind, h->merid);
+      if (rc) return rc;
+    }
+  }
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+int ccs_step(ccs_handle *h, int nsteps) {
+  if (!h || nsteps < 0) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (h->cfg.precision == CCS_MIXED) return mixed_step(h, nsteps, true);
+  return f64_step(h, nsteps, true);
+}
+
+int ccs_step_async(ccs_handle *h, int nsteps) {
+  if (!h || nsteps < 0) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (h->cfg.precision == CCS_MIXED) return mixed_step(h, nsteps, false);
+  return f64_step(h, nsteps, false);
+}
+
+int ccs_sync(ccs_handle *h) {
+  if (!h) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+int ccs_spatial_operator(ccs_handle *h, double *tp, double *tu, double *tv) {
+  if (!h) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (h->cfg.precision == CCS_MIXED) return mixed_tend(h, tp, tu, tv);
+  const F64Stage *d = h->d_stages + h->n_rk + 1;
+  CCS_TRY(h, launch_f64_stage(d, h->d_work, h->nwork, h->grid, h->stream));
+  double *dst[3] = {tp, tu, tv};
+  for (int k = 0; k < 3; k++)
+    if (dst[k]) {
+      int rc = download_field(h, dst[k], h->tend[k]);
+      if (rc) return rc;
+    }
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+int ccs_diag(ccs_handle *h, double *mass, double *energy) {
+  if (!h) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (h->cfg.precision == CCS_MIXED) return mixed_diag(h, mass, energy);
+  const MeshF64 &m = h->mesh->m64;
+  CCS_TRY(h, launch_f64_diag(h->L, h->S[0].phiG, h->S[0].phi, h->S[0].u, h->S[0].v, h->S[0].uC, h->S[0].vC,
+                             m.sqrtG, m.phis, h->d_partials, kDiagBlocks, h->stream));
+  std::vector<double> part(2 * kDiagBlocks);
+  CCS_TRY(h, cudaMemcpyAsync(part.data(), h->d_partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  double tm = 0., te = 0.;
+  for (int b = 0; b < kDiagBlocks; b++) {
+    tm += part[2 * b];
+    te += part[2 * b + 1];
+  }
+  if (mass) *mass = tm;
+  if (energy) *energy = te;
+  return CCS_OK;
+}
+
+int ccs_timing(ccs_handle *h, int enable, int reset, double *kernel_ms, int64_t *launches) {
+  if (!h) return CCS_ERR_ARG;
+  if (kernel_ms) *kernel_ms = h->kernel_ms;
+  if (launches) *launches = h->launches;
+  if (reset) {
+    h->kernel_ms = 0.;
+    h->launches = 0;
+  }
+  if (enable >= 0) h->timing = enable != 0;
+  return CCS_OK;
+}
+
+}  // extern "C"
+
+
+// ---------------------------------------------------------------------------
+// mixed lane host side
+// ---------------------------------------------------------------------------
+struct MixedLane {
+  float *buf = nullptr;  // S[3] (3 fields each), lo(3), acc(3), tend(3)
+  StateMixed S[3]{};
+  float *lo[3]{}, *acc[3]{}, *tend[3]{};
+  double *staging = nullptr;  // 8 reference-layout FP64 fields
+  std::vector<MixedStage> h_stages;
+  MixedStage *d_stages = nullptr;
+  int n_rk = 0;
+  WorkItem *d_work = nullptr;
+  int nwork = 0, grid = 0;
+  double phibar = 0.;
+  bool have_phibar = false;
+  cudaGraphExec_t g_step = nullptr;
+};
+
+static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *mv) {
+  const Layout &L = h->L;
+  const int N = L.N, hh = L.h, nh = L.nh;
+  const double a2 = h->cfg.radius * h->cfg.radius;
+  const size_t nf = (size_t)L.field, np = (size_t)L.panel;
+  const size_t nref = (size_t)nh * nh * 6;
+  // shared: s ig11 ig12 ig21 ig22 inv_s (one panel each); per panel: phis fs
+  const size_t nfloat = 6 * np + 2 * nf;
+  CCS_TRY(h, cudaMalloc(&dm->buf32, nfloat * sizeof(float)));
+  std::vector<float> hb(nfloat, 0.f);
+  float *sh[6];
+  for (int k = 0; k < 6; k++) sh[k] = hb.data() + k * np;
+  float *phs = hb.data() + 6 * np, *fs = phs + nf;
+  for (int p = 0; p < 6; p++)
+    for (int j = 1 - hh; j <= N + hh; j++)
+      for (int i = 1 - hh; i <= N + hh; i++) {
+        const size_t r = (size_t)(i + hh - 1) + (size_t)nh * ((size_t)(j + hh - 1) + (size_t)nh * p);
+        const int64_t d = L.idx(i, j, p);
+        const double sg = mv->sqrtG[r];
+        if (p == 0) {
+          const double *IG = &mv->matrixIG[4 * r];
+          sh[0][d] = (float)(sg / a2);
+          sh[1][d] = (float)(IG[0] * a2);
+          sh[2][d] = (float)(IG[2] * a2);
+          sh[3][d] = (float)(IG[1] * a2);
+          sh[4][d] = (float)(IG[3] * a2);
+          sh[5][d] = sg > 0. ? (float)(a2 / sg) : 0.f;
+        }
+        phs[d] = (float)mv->phis[r];
+        fs[d] = (float)(mv->f[r] * sg / a2);
+      }
+  CCS_TRY(h, cudaMemcpyAsync(dm->buf32, hb.data(), nfloat * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  // FP64 halo transforms, one per push-table entry: T = (G IA)_halo (A IG)_source
+  const size_t ne = (size_t)24 * hh * N;
+  std::vector<double> xf(4 * ne, 0.);
+  for (int p = 1; p <= 6; p++)
+    for (int side = 0; side < 4; side++)
+      for (int k = 1; k <= hh; k++)
+        for (int m = 1; m <= N; m++) {
+          const GhostSrc s = ghost_source(N, p, side, k, m);
+          const int ss = ghost_source_side(p, side);
+          int di, dj;
+          switch (side) {
+            case 0: di = 1 - k; dj = m; break;
+            case 1: di = N + k; dj = m; break;
+            case 2: di = m; dj = 1 - k; break;
+            default: di = m; dj = N + k; break;
+          }
+          int ks, ms;
+          switch (ss) {
+            case 0: ks = s.i; ms = s.j; break;
+            case 1: ks = N + 1 - s.i; ms = s.j; break;
+            case 2: ks = s.j; ms = s.i; break;
+            default: ks = N + 1 - s.j; ms = s.i; break;
+          }
+          const size_t e = ((size_t)(s.p - 1) * 4 + ss) * hh * N + (size_t)(ks - 1) * N + (ms - 1);
+          const size_t rd = (size_t)(di + hh - 1) + (size_t)nh * ((size_t)(dj + hh - 1) + (size_t)nh * (p - 1));
+          const size_t rs =
+              (size_t)(s.i + hh - 1) + (size_t)nh * ((size_t)(s.j + hh - 1) + (size_t)nh * (s.p - 1));
+          double GIA[4], AIG[4], T[4];
+          matmul22(&mv->matrixG[4 * rd], &mv->matrixIA[4 * rd], GIA);
+          matmul22(&mv->matrixA[4 * rs], &mv->matrixIG[4 * rs], AIG);
+          matmul22(GIA, AIG, T);
+          xf[4 * e + 0] = T[0];  // T(1,1)
+          xf[4 * e + 1] = T[2];  // T(1,2)
+          xf[4 * e + 2] = T[1];  // T(2,1)
+          xf[4 * e + 3] = T[3];  // T(2,2)
+        }
+  double *dxf = nullptr;
+  // the transforms live after the FP64 mesh arrays in their own allocation
+  CCS_TRY(h, cudaMalloc(&dxf, xf.size() * sizeof(double)));
+  CCS_TRY(h, cudaMemcpyAsync(dxf, xf.data(), xf.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  dm->xf = dxf;
+  dm->mm.s = dm->buf32;
+  dm->mm.ig11 = dm->buf32 + np;
+  dm->mm.ig12 = dm->buf32 + 2 * np;
+  dm->mm.ig21 = dm->buf32 + 3 * np;
+  dm->mm.ig22 = dm->buf32 + 4 * np;
+  dm->mm.inv_s = dm->buf32 + 5 * np;
+  dm->mm.phis = dm->buf32 + 6 * np;
+  dm->mm.fs = dm->buf32 + 6 * np + nf;
+  dm->mm.xf = dxf;
+  dm->mm.push = dm->push;
+  (void)nref;
+  return CCS_OK;
+}
+
+static int mixed_handle_create(ccs_handle *h) {
+  MixedLane *M = new MixedLane();
+  h->mixed = M;
+  const Layout &L = h->L;
+  const size_t nf = (size_t)L.field;
+  const size_t nref = (size_t)L.nh * L.nh * 6;
+  CCS_TRY(h, cudaMalloc(&M->buf, 18 * nf * sizeof(float)));
+  CCS_TRY(h, cudaMemsetAsync(M->buf, 0, 18 * nf * sizeof(float), h->stream));
+  float *b = M->buf;
+  for (int s = 0; s < 3; s++) {
+    M->S[s].hp = b; b += nf;
+    M->S[s].u = b; b += nf;
+    M->S[s].v = b; b += nf;
+  }
+  for (int k = 0; k < 3; k++) { M->lo[k] = b; b += nf; }
+  for (int k = 0; k < 3; k++) { M->acc[k] = b; b += nf; }
+  for (int k = 0; k < 3; k++) { M->tend[k] = b; b += nf; }
+  CCS_TRY(h, cudaMalloc(&M->staging, 8 * nref * sizeof(double)));
+  CCS_TRY(h, cudaMalloc(&h->d_partials, 2 * kDiagBlocks * sizeof(double)));
+  // work list
+  const int ntx = (L.N + MX_TX - 1) / MX_TX, nty = (L.N + MX_TY - 1) / MX_TY;
+  std::vector<WorkItem> work;
+  for (int p = 0; p < 6; p++)
+    for (int ty = 0; ty < nty; ty++)
+      for (int tx = 0; tx < ntx; tx++) work.push_back(WorkItem{0, (int16_t)p, (int16_t)tx, (int16_t)ty});
+  M->nwork = (int)work.size();
+  CCS_TRY(h, cudaMalloc(&M->d_work, work.size() * sizeof(WorkItem)));
+  CCS_TRY(h, cudaMemcpyAsync(M->d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                             h->stream));
+  M->grid = mixed_max_grid(h->cfg.device);
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+// (re)build the stage descriptors once phibar is known
+static int mixed_build_stages(ccs_handle *h) {
+  MixedLane *M = h->mixed;
+  const ccs_config &c = h->cfg;
+  const double a2 = c.radius * c.radius;
+  MixedStage base{};
+  base.L = h->L;
+  base.m = h->mesh->mm;
+  base.y0hp = M->S[0].hp; base.y0u = M->S[0].u; base.y0v = M->S[0].v;
+  base.lohp = M->lo[0]; base.lou = M->lo[1]; base.lov = M->lo[2];
+  base.acchp = M->acc[0]; base.accu = M->acc[1]; base.accv = M->acc[2];
+  base.rdx = (float)(1. / c.dx); base.rdy = (float)(1. / c.dy);
+  base.rdx60 = (float)(1. / (60. * c.dx)); base.rdy60 = (float)(1. / (60. * c.dy));
+  base.phibar = (float)M->phibar;
+  base.a2 = (float)a2;
+  base.inv_a2 = (float)(1. / a2);
+  base.eps_E = 1.e-2f;
+  base.eps_F = (float)(1.e-2 / (a2 * a2));
+  base.eps_P = (float)(1.e-2 / (a2 * a2));
+  base.ediss = c.e_dissipation;
+  auto mk = [&](int kind, int in, int out, double c1) {
+    MixedStage s = base;
+    s.kind = kind;
+    s.in = M->S[in];
+    s.out = M->S[out];
+    s.c1 = (float)c1;
+    return s;
+  };
+  M->h_stages.clear();
+  const double dt = c.dt;
+  if (c.scheme == CCS_RK4) {
+    M->n_rk = 4;
+    M->h_stages.push_back(mk(K_RK4_1, 0, 1, 0.5 * dt));
+    M->h_stages.push_back(mk(K_RK4_2, 1, 2, 0.5 * dt));
+    M->h_stages.push_back(mk(K_RK4_2, 2, 1, dt));
+    M->h_stages.push_back(mk(K_RK4_4, 1, 0, dt));
+  } else {
+    M->n_rk = 3;
+    M->h_stages.push_back(mk(K_RK3_1, 0, 1, dt));
+    M->h_stages.push_back(mk(K_RK3_2, 1, 2, 0.25 * dt));
+    M->h_stages.push_back(mk(K_RK3_3, 2, 0, 2. / 3. * dt));
+  }
+  MixedStage td = mk(K_TEND, 0, 0, 0.);
+  td.thp = M->tend[0]; td.tu = M->tend[1]; td.tv = M->tend[2];
+  M->h_stages.push_back(td);
+  if (!M->d_stages) CCS_TRY(h, cudaMalloc(&M->d_stages, 8 * sizeof(MixedStage)));
+  CCS_TRY(h, cudaMemcpyAsync(M->d_stages, M->h_stages.data(), M->h_stages.size() * sizeof(MixedStage),
+                             cudaMemcpyHostToDevice, h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  if (M->g_step) {
+    cudaGraphExecDestroy(M->g_step);
+    M->g_step = nullptr;
+  }
+  return CCS_OK;
+}
+
+static void mixed_handle_destroy(ccs_handle *h) {
+  MixedLane *M = h->mixed;
+  if (!M) return;
+  if (M->g_step) cudaGraphExecDestroy(M->g_step);
+  if (M->buf) cudaFree(M->buf);
+  if (M->staging) cudaFree(M->staging);
+  if (M->d_stages) cudaFree(M->d_stages);
+  if (M->d_work) cudaFree(M->d_work);
+  delete M;
+  h->mixed = nullptr;
+}
+
+static int mixed_set_state(ccs_handle *h, const ccs_state_view *s) {
+  MixedLane *M = h->mixed;
+  const Layout &L = h->L;
+  const size_t nref = (size_t)L.nh * L.nh * 6;
+  if (!M->have_phibar) {
+    double phibar = h->cfg.phi_mean;
+    if (!(phibar > 0.)) {
+      double acc = 0.;
+      for (int p = 0; p < 6; p++)
+        for (int j = 1; j <= L.N; j++)
+          for (int i = 1; i <= L.N; i++)
+            acc += s->phi[(size_t)(i + L.h - 1) + (size_t)L.nh * ((size_t)(j + L.h - 1) + (size_t)L.nh * p)];
+      phibar = acc / (6. * L.N * L.N);
+    }
+    M->phibar = phibar;
+    M->have_phibar = true;
+    int rc = mixed_build_stages(h);
+    if (rc) return rc;
+  }
+  double *st = M->staging;
+  CCS_TRY(h, cudaMemcpyAsync(st, s->phi, nref * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CCS_TRY(h, cudaMemcpyAsync(st + nref, s->u, nref * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CCS_TRY(h, cudaMemcpyAsync(st + 2 * nref, s->v, nref * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  const double a2 = h->cfg.radius * h->cfg.radius;
+  CCS_TRY(h, launch_mixed_import(L, st, st + nref, st + 2 * nref, M->phibar, 1. / a2, M->S[0], M->lo[0],
+                                 M->lo[1], M->lo[2], h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+static int mixed_get_state(ccs_handle *h, ccs_state_view *s) {
+  MixedLane *M = h->mixed;
+  if (!M->have_phibar) return CCS_ERR_ARG;
+  const Layout &L = h->L;
+  const size_t nref = (size_t)L.nh * L.nh * 6;
+  double *out[8];
+  for (int k = 0; k < 8; k++) out[k] = M->staging + k * nref;
+  const double a2 = h->cfg.radius * h->cfg.radius;
+  CCS_TRY(h, launch_mixed_export(L, M->S[0], M->lo[0], M->lo[1], M->lo[2], h->mesh->m64, M->phibar, a2, out,
+                                 h->stream));
+  double *dst[8] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC, s->zonal_wind, s->meridional_wind};
+  for (int k = 0; k < 8; k++)
+    if (dst[k])
+      CCS_TRY(h, cudaMemcpyAsync(dst[k], out[k], nref * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+static int mixed_enqueue_step(ccs_handle *h) {
+  MixedLane *M = h->mixed;
+  for (int k = 0; k < M->n_rk; k++) {
+    if (h->timing) CCS_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    CCS_TRY(h, launch_mixed_stage(M->d_stages + k, M->d_work, M->nwork, M->grid, h->stream));
+    if (h->timing) {
+      CCS_TRY(h, cudaEventRecord(h->ev1, h->stream));
+      CCS_TRY(h, cudaEventSynchronize(h->ev1));
+      float ms = 0.f;
+      CCS_TRY(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+      h->kernel_ms += ms;
+      h->launches++;
+    }
+  }
+  return CCS_OK;
+}
+
+static int mixed_step(ccs_handle *h, int nsteps, bool sync) {
+  MixedLane *M = h->mixed;
+  if (!M->have_phibar) return CCS_ERR_ARG;
+  if (nsteps <= 0) return CCS_OK;
+  if (h->timing) {
+    for (int s = 0; s < nsteps; s++) {
+      int rc = mixed_enqueue_step(h);
+      if (rc) return rc;
+    }
+  } else {
+    if (!M->g_step) {
+      cudaGraph_t g = nullptr;
+      CCS_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = mixed_enqueue_step(h);
+      cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+      if (rc) return rc;
+      CCS_TRY(h, e);
+      e = cudaGraphInstantiate(&M->g_step, g, 0);
+      cudaGraphDestroy(g);
+      CCS_TRY(h, e);
+    }
+    for (int s = 0; s < nsteps; s++) CCS_TRY(h, cudaGraphLaunch(M->g_step, h->stream));
+  }
+  if (sync) CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv) {
+  MixedLane *M = h->mixed;
+  if (!M->have_phibar) return CCS_ERR_ARG;
+  const Layout &L = h->L;
+  const size_t nref = (size_t)L.nh * L.nh * 6;
+  CCS_TRY(h, launch_mixed_stage(M->d_stages + M->n_rk, M->d_work, M->nwork, M->grid, h->stream));
+  const double a2 = h->cfg.radius * h->cfg.radius;
+  double *o = M->staging;
+  CCS_TRY(h, launch_mixed_tend_export(L, M->tend[0], M->tend[1], M->tend[2], h->mesh->m64, a2, o, o + nref,
+                                      o + 2 * nref, h->stream));
+  double *dst[3] = {tp, tu, tv};
+  for (int k = 0; k < 3; k++)
+    if (dst[k])
+      CCS_TRY(h, cudaMemcpyAsync(dst[k], o + k * nref, nref * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
+static int mixed_diag(ccs_handle *h, double *mass, double *energy) {
+  MixedLane *M = h->mixed;
+  if (!M->have_phibar) return CCS_ERR_ARG;
+  const double a2 = h->cfg.radius * h->cfg.radius;
+  CCS_TRY(h, launch_mixed_diag(h->L, M->S[0], M->lo[0], M->lo[1], M->lo[2], h->mesh->m64, M->phibar, a2,
+                               h->d_partials, kDiagBlocks, h->stream));
+  std::vector<double> part(2 * kDiagBlocks);
+  CCS_TRY(h, cudaMemcpyAsync(part.data(), h->d_partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  double tm = 0., te = 0.;
+  for (int b = 0; b < kDiagBlocks; b++) {
+    tm += part[2 * b];
+    te += part[2 * b + 1];
+  }
+  if (mass) *mass = tm;
+  if (energy) *energy = te;
+  return CCS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batches: one launch per lane and RK stage over the union of the members' tiles
+// ---------------------------------------------------------------------------
+struct BatchGroup {
+  int lane = 0, n_rk = 0, nmem = 0;
+  std::vector<ccs_handle *> members;
+  void *d_stages = nullptr;  // [n_rk + 1][nmem] F64Stage or MixedStage (last row: F64 final with sphere winds)
+  WorkItem *d_work = nullptr;
+  int nwork = 0, grid = 0;
+};
+
+struct ccs_batch {
+  std::vector<BatchGroup> groups;
+  std::vector<ccs_handle *> members;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  cudaGraphExec_t g_step = nullptr, g_step_sw = nullptr;
+  std::string err;
+};
+
+static int batch_enqueue(ccs_batch *b, bool with_sw) {
+  const int maxrk = 4;
+  for (int k = 0; k < maxrk; k++)
+    for (auto &g : b->groups) {
+      if (k >= g.n_rk) continue;
+      cudaError_t e;
+      if (g.lane == CCS_FP64) {
+        const int row = (k == g.n_rk - 1 && with_sw) ? g.n_rk : k;
+        e = launch_f64_stage((const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork, g.grid,
+                             b->stream);
+      } else {
+        e = launch_mixed_stage((const MixedStage *)g.d_stages + (size_t)k * g.nmem, g.d_work, g.nwork, g.grid,
+                               b->stream);
+      }
+      if (e != cudaSuccess) {
+        b->err = cudaGetErrorString(e);
+        return CCS_ERR_CUDA;
+      }
+    }
+  return CCS_OK;
+}
+
+extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out) {
+  if (!members || n < 1 || !out) return CCS_ERR_ARG;
+  *out = nullptr;
+  const int dev = members[0]->cfg.device;
+  for (int k = 0; k < n; k++) {
+    if (!members[k] || members[k]->cfg.device != dev) return CCS_ERR_ARG;
+    if (members[k]->cfg.precision == CCS_MIXED && !members[k]->mixed->have_phibar) return CCS_ERR_ARG;
+  }
+  if (n > 32767) return CCS_ERR_ARG;
+  cudaSetDevice(dev);
+  ccs_batch *b = new ccs_batch();
+  b->device = dev;
+  b->members.assign(members, members + n);
+  cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  for (int lane = 0; lane < 2; lane++)
+    for (int scheme = 0; scheme < 2; scheme++) {
+      BatchGroup g;
+      g.lane = lane;
+      for (int k = 0; k < n; k++)
+        if (members[k]->cfg.precision == lane && members[k]->cfg.scheme == scheme) g.members.push_back(members[k]);
+      if (g.members.empty()) continue;
+      g.nmem = (int)g.members.size();
+      g.n_rk = scheme == CCS_RK4 ? 4 : 3;
+      std::vector<WorkItem> work;
+      const int TXg = lane == CCS_FP64 ? F64_TX : MX_TX, TYg = lane == CCS_FP64 ? F64_TY : MX_TY;
+      for (int m = 0; m < g.nmem; m++) {
+        const int N = g.members[m]->cfg.N;
+        const int ntx = (N + TXg - 1) / TXg, nty = (N + TYg - 1) / TYg;
+        for (int p = 0; p < 6; p++)
+          for (int ty = 0; ty < nty; ty++)
+            for (int tx = 0; tx < ntx; tx++)
+              work.push_back(WorkItem{(int16_t)m, (int16_t)p, (int16_t)tx, (int16_t)ty});
+      }
+      g.nwork = (int)work.size();
+      cudaMalloc(&g.d_work, work.size() * sizeof(WorkItem));
+      cudaMemcpy(g.d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice);
+      if (lane == CCS_FP64) {
+        std::vector<F64Stage> st((size_t)(g.n_rk + 1) * g.nmem);
+        for (int k = 0; k <= g.n_rk; k++)
+          for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->h_stages[k];
+        cudaMalloc(&g.d_stages, st.size() * sizeof(F64Stage));
+        cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(F64Stage), cudaMemcpyHostToDevice);
+        g.grid = f64_max_grid(dev, 1);
+      } else {
+        std::vector<MixedStage> st((size_t)g.n_rk * g.nmem);
+        for (int k = 0; k < g.n_rk; k++)
+          for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->mixed->h_stages[k];
+        cudaMalloc(&g.d_stages, st.size() * sizeof(MixedStage));
+        cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(MixedStage), cudaMemcpyHostToDevice);
+        g.grid = mixed_max_grid(dev);
+      }
+      b->groups.push_back(g);
+    }
+  if (cudaGetLastError() != cudaSuccess) {
+    ccs_batch_destroy(b);
+    return CCS_ERR_CUDA;
+  }
+  *out = b;
+  return CCS_OK;
+}
+
+static int batch_capture(ccs_batch *b, bool with_sw, cudaGraphExec_t *out) {
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CCS_ERR_CUDA;
+  int rc = batch_enqueue(b, with_sw);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return CCS_ERR_CUDA;
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  return e == cudaSuccess ? CCS_OK : CCS_ERR_CUDA;
+}
+
+extern "C" int ccs_batch_step(ccs_batch *b, int nsteps) {
+  if (!b || nsteps < 0) return CCS_ERR_ARG;
+  if (nsteps == 0) return CCS_OK;
+  cudaSetDevice(b->device);
+  // members' own streams may hold pending work (set_state is synchronous, so
+  // nothing is pending here); the batch runs on its own stream
+  if (!b->g_step) {
+    int rc = batch_capture(b, false, &b->g_step);
+    if (!rc) rc = batch_capture(b, true, &b->g_step_sw);
+    if (rc) return rc;
+  }
+  for (int s = 0; s < nsteps - 1; s++)
+    if (cudaGraphLaunch(b->g_step, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  if (cudaGraphLaunch(b->g_step_sw, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  for (ccs_handle *h : b->members) h->sphere_valid = true;
+  return CCS_OK;
+}
+
+extern "C" void ccs_batch_destroy(ccs_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->g_step) cudaGraphExecDestroy(b->g_step);
+  if (b->g_step_sw) cudaGraphExecDestroy(b->g_step_sw);
+  for (auto &g : b->groups) {
+    if (g.d_stages) cudaFree(g.d_stages);
+    if (g.d_work) cudaFree(g.d_work);
+  }
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}

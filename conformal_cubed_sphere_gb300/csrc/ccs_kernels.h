@@ -1,0 +1,93 @@
+// ccs_kernels.h -- launch descriptors shared by the kernels and the C ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ccs_internal.h"
+
+namespace ccs {
+
+// One tile of work: instance, panel (0..5) and tile coordinates.
+struct WorkItem {
+  int16_t inst, panel, tx, ty;
+};
+
+// Stage kinds.  RK4 (time_scheme_mod.F90:13-44) keeps the running combination
+// acc = k1 (+ 2 k2) (+ 2 k3) so that the final (acc + k4) / 6 has the reference's
+// association ((k1 + 2k2) + 2k3) + k4.  RK3-TVD follows :46-67, 85-115.
+enum StageKind {
+  K_RK4_1 = 0,  // acc = k;          Y = Y0 + c1 k
+  K_RK4_2 = 1,  // acc = acc + 2 k;  Y = Y0 + c1 k
+  K_RK4_4 = 2,  // Y = Y0 + c1 ((acc + k) / 6)
+  K_RK3_1 = 3,  // Y = Y0 + c1 k
+  K_RK3_2 = 4,  // Y = 0.75 Y0 + 0.25 Yc + c1 k
+  K_RK3_3 = 5,  // Y = Y0 / 3 + 2/3 Yc + c1 k
+  K_TEND = 6    // write k only
+};
+
+// FP64 lane: everything one instance's stage launch needs.
+struct F64Stage {
+  Layout L;
+  MeshF64 m;
+  StateF64 in;   // stencil input Y_k
+  StateF64 out;  // Y_{k+1} (may alias the Y0 slot: only the own cell of Y0 is read)
+  const double *y0phiG, *y0u, *y0v;
+  double *accphiG, *accu, *accv;
+  double *zonal, *merid;  // sphere winds of Y_{k+1} when non-null
+  double *tphiG, *tu, *tv;
+  double dx, dy, dx60, dy60, c1;
+  int kind, ediss;
+};
+
+// Mixed lane: one instance's stage launch.
+struct MixedStage {
+  Layout L;
+  MeshMixed m;
+  StateMixed in, out;
+  const float *y0hp, *y0u, *y0v;
+  float *lohp, *lou, *lov;  // compensation terms of the step-to-step state (interior)
+  float *acchp, *accu, *accv;
+  float *thp, *tu, *tv;
+  float rdx, rdy, rdx60, rdy60;  // reciprocals of dx, dy, 60 dx, 60 dy
+  float c1;
+  float phibar;  // mean geopotential phibar (m^2 s^-2)
+  float a2, inv_a2;
+  float eps_E;  // WENO eps of E (m^2 s^-2 units: the reference's 1e-2)
+  float eps_F;  // eps of the flux / a^2 (1e-2 / a^4)
+  float eps_P;  // eps of phitG / a^2 (1e-2 / a^4)
+  int kind, ediss;
+};
+
+// kernel launchers (return cudaGetLastError())
+cudaError_t launch_f64_stage(const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid,
+                             cudaStream_t s);
+int f64_stage_smem_bytes(int ediss);
+int f64_max_grid(int device, int ediss);
+
+cudaError_t launch_mixed_stage(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid,
+                               cudaStream_t s);
+int mixed_max_grid(int device);
+int mixed_smem_bytes();
+cudaError_t launch_mixed_import(const Layout &L, const double *phi, const double *u, const double *v,
+                                double phibar, double inv_a2, StateMixed out, float *lohp, float *lou,
+                                float *lov, cudaStream_t s);
+cudaError_t launch_mixed_export(const Layout &L, StateMixed st, const float *lohp, const float *lou,
+                                const float *lov, const MeshF64 &m, double phibar, double a2, double *const out[8],
+                                cudaStream_t s);
+cudaError_t launch_mixed_tend_export(const Layout &L, const float *thp, const float *tu, const float *tv,
+                                     const MeshF64 &m, double a2, double *op, double *ou, double *ov,
+                                     cudaStream_t s);
+cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp, const float *lou,
+                              const float *lov, const MeshF64 &m, double phibar, double a2, double *partials,
+                              int nblocks, cudaStream_t s);
+
+// tile shapes
+constexpr int F64_TX = 32, F64_TY = 8, F64_THREADS = 256;
+constexpr int MX_TX = 32, MX_TY = 16, MX_THREADS = 256;
+
+// FP64 reductions (mass / energy) over the interior of an FP64 state
+cudaError_t launch_f64_diag(const Layout &L, const double *phiG, const double *phi, const double *u,
+                            const double *v, const double *uC, const double *vC, const double *sqrtG,
+                            const double *phis, double *partials, int nblocks, cudaStream_t s);
+
+}  // namespace ccs

@@ -1,0 +1,486 @@
+// ccs_mixed.cu -- mixed-precision lane: FP32 state and stencil arithmetic, FP64
+// cross-panel vector transforms, FP64 import / export / diagnostics.
+//
+// State per cell: hp = phi - phibar (geopotential of the fluid depth minus a fixed
+// mean), u~ = u / a^2, v~ = v / a^2 (covariant wind), FP32; the step-to-step state
+// also carries an FP32 compensation term per field (Kahan update of the final RK
+// stage).  Metric: the cube map's metric tensor is the same on all six panels
+// (halo included), so one FP32 copy of s = sqrtG / a^2 and ig = IG a^2 serves
+// every panel and stays L2-resident; phis and f s are per panel.
+//
+// The WENO-Z reconstructions are written in difference form: WENO is invariant
+// under adding a constant to its five inputs, so every quantity of the flux
+// formula of spatial_operators_mod.F90:101-179 is expressed through the
+// differences d_k = Q_{k+1} - Q_k of neighbouring cells and the corrections
+// D = Rec - Q_c.  The large mean parts (phibar of phit, phibar s of phitG) cancel
+// before rounding instead of after; the weights are the reference's WENO-Z
+// weights with eps rescaled to the non-dimensional fields.
+#include "ccs_kernels.h"
+
+namespace ccs {
+
+namespace {
+
+constexpr int TX = MX_TX, TY = MX_TY, NT = MX_THREADS;
+constexpr int RX = TX + 6, RY = TY + 6, RN = RX * RY;
+constexpr int NCX = TY * (TX + 2), NCY = TX * (TY + 2), NC2 = NCX + NCY;
+constexpr int NFX = TY * (TX + 1), NFY = (TY + 1) * TX;
+
+// Difference-form WENO-Z (spatial_operators_mod.F90:282-361) of one cell for both
+// directions.  d0..d3 = Q(c-1)-Q(c-2), Q(c)-Q(c-1), Q(c+1)-Q(c), Q(c+2)-Q(c+1).
+// Returns Dp = Rec+(c) - Q(c) (face c+1/2) and Dm = Rec-(c) - Q(c) (face c-1/2).
+// The "-" smoothness indicators are the "+" ones mirrored (beta'_k = beta_{4-k}),
+// so the three divisions tau5 / (eps + beta_k) are shared.
+__device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, float eps, float &Dp,
+                                       float &Dm) {
+  const float A1 = d1 - d0, A2 = d2 - d1, A3 = d3 - d2;
+  const float B1 = fmaf(3.f, d1, -d0), B2 = d1 + d2, B3 = fmaf(-3.f, d2, d3);
+  const float c1312 = 13.f / 12.f;
+  const float b1 = fmaf(c1312 * A1, A1, 0.25f * B1 * B1);
+  const float b2 = fmaf(c1312 * A2, A2, 0.25f * B2 * B2);
+  const float b3 = fmaf(c1312 * A3, A3, 0.25f * B3 * B3);
+  const float t40 = fabsf(b1 - b2), t41 = fabsf(b2 - b3), t5 = fabsf(b3 - b1);
+  const float mn = fminf(b1, fminf(b2, b3));
+  const float r1 = __fdividef(t5, eps + b1);
+  const float r2 = __fdividef(t5, eps + b2);
+  const float r3 = __fdividef(t5, eps + b3);
+  // candidate corrections S_k - Q(c)
+  const float p1 = fmaf(5.f / 6.f, d1, -(1.f / 3.f) * d0);
+  const float p2 = fmaf(1.f / 6.f, d1, (1.f / 3.f) * d2);
+  const float p3 = fmaf(2.f / 3.f, d2, -(1.f / 6.f) * d3);
+  const float m1 = fmaf(-5.f / 6.f, d2, (1.f / 3.f) * d3);
+  const float m2 = fmaf(-1.f / 6.f, d2, -(1.f / 3.f) * d1);
+  const float m3 = fmaf(-2.f / 3.f, d1, (1.f / 6.f) * d0);
+  // "+" weights
+  {
+    const float a1 = 0.1f + 0.1f * r1, a2 = 0.6f + 0.6f * r2, a3 = 0.3f + 0.3f * r3;
+    float num = fmaf(a1, p1, fmaf(a2, p2, a3 * p3));
+    float val = __fdividef(num, a1 + a2 + a3);
+    if (t40 <= mn && t41 > mn) val = fmaf(1.f / 3.f, p1, (2.f / 3.f) * p2);
+    else if (t40 > mn && t41 < mn) val = fmaf(2.f / 3.f, p2, (1.f / 3.f) * p3);
+    Dp = val;
+  }
+  // "-" weights: beta' = (b3, b2, b1), tau40' = t41, tau41' = t40
+  {
+    const float a1 = 0.1f + 0.1f * r3, a2 = 0.6f + 0.6f * r2, a3 = 0.3f + 0.3f * r1;
+    float num = fmaf(a1, m1, fmaf(a2, m2, a3 * m3));
+    float val = __fdividef(num, a1 + a2 + a3);
+    if (t41 <= mn && t40 > mn) val = fmaf(1.f / 3.f, m1, (2.f / 3.f) * m2);
+    else if (t41 > mn && t40 < mn) val = fmaf(2.f / 3.f, m2, (1.f / 3.f) * m3);
+    Dm = val;
+  }
+}
+
+struct SmemMx {
+  float uC[RN], vC[RN], F[RN], G[RN], E[RN], q[RN], s[RN], phit[RN], ig11[RN], ig22[RN], u[RN], v[RN];
+  float Dx[6][NCX];  // (DFp, DFm, DEp, DEm, DPp, DPm) at x-cells
+  float Dy[6][NCY];
+  float gx[2][NFX];  // (flux, E) face values relative to the left cell
+  float gy[2][NFY];
+};
+
+__device__ __forceinline__ bool corner(int i, int j, int N) { return (i < 1 || i > N) && (j < 1 || j > N); }
+
+__global__ void __launch_bounds__(NT, 2)
+mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
+  extern __shared__ __align__(16) float smem_f[];
+  SmemMx &S = *reinterpret_cast<SmemMx *>(smem_f);
+  const int tid = threadIdx.x;
+
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const WorkItem wi = work[w];
+    const MixedStage &st = stages[wi.inst];
+    const Layout L = st.L;
+    const int N = L.N, p = wi.panel;
+    const int i0 = 1 + wi.tx * TX, j0 = 1 + wi.ty * TY;
+    const float phibar = st.phibar;
+    const float a2 = st.a2;
+
+    // ---- phase 1: cell quantities -----------------------------------------
+    for (int r = tid; r < RN; r += NT) {
+      const int li = r % RX, lj = r / RX;
+      const int i = i0 - 3 + li, j = j0 - 3 + lj;
+      float uC = 0.f, vC = 0.f, F = 0.f, G = 0.f, E = 0.f, q = 0.f, s = 1.f, pt = 0.f, g11 = 0.f, g22 = 0.f,
+            u = 0.f, v = 0.f;
+      if (i >= -2 && i <= N + 3 && j >= -2 && j <= N + 3 && !corner(i, j, N)) {
+        const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
+        const float hp = st.in.hp[c];
+        u = st.in.u[c];
+        v = st.in.v[c];
+        const float phs = st.m.phis[c];
+        s = st.m.s[cs];
+        g11 = st.m.ig11[cs];
+        g22 = st.m.ig22[cs];
+        const float g12 = st.m.ig12[cs], g21 = st.m.ig21[cs];
+        uC = fmaf(g11, u, g12 * v);
+        vC = fmaf(g21, u, g22 * v);
+        const float mass = (phibar + hp) * s;  // phiG / a^2
+        F = mass * uC;
+        G = mass * vC;
+        const float hs = phs + hp;
+        E = fmaf(0.5f * a2, fmaf(u, uC, v * vC), hs);  // E - phibar
+        q = hs * s;                                     // phitG / a^2 - phibar s
+        pt = phibar + hs;
+      }
+      S.uC[r] = uC; S.vC[r] = vC; S.F[r] = F; S.G[r] = G; S.E[r] = E; S.q[r] = q; S.s[r] = s;
+      S.phit[r] = pt; S.ig11[r] = g11; S.ig22[r] = g22; S.u[r] = u; S.v[r] = v;
+    }
+    __syncthreads();
+
+    // ---- phase 2: difference-form WENO at cells ------------------------------
+    for (int t = tid; t < 3 * NC2; t += NT) {
+      const int fld = t / NC2, rem = t % NC2;
+      int r, stp, ok;
+      if (rem < NCX) {
+        const int ci = rem % (TX + 2), lj = rem / (TX + 2);
+        const int i = i0 - 1 + ci, j = j0 + lj;
+        ok = (i <= N + 1) && (j <= N);
+        r = (lj + 3) * RX + ci + 2;
+        stp = 1;
+      } else {
+        const int rr = rem - NCX;
+        const int li = rr % TX, cj = rr / TX;
+        const int i = i0 + li, j = j0 - 1 + cj;
+        ok = (i <= N) && (j <= N + 1);
+        r = (cj + 2) * RX + li + 3;
+        stp = RX;
+      }
+      float Dp = 0.f, Dm = 0.f;
+      if (ok) {
+        float d0, d1, d2, d3, eps;
+        if (fld == 2) {  // phitG: d = phibar ds + dq
+          const float *sq = S.q, *ss = S.s;
+          d0 = fmaf(phibar, ss[r - stp] - ss[r - 2 * stp], sq[r - stp] - sq[r - 2 * stp]);
+          d1 = fmaf(phibar, ss[r] - ss[r - stp], sq[r] - sq[r - stp]);
+          d2 = fmaf(phibar, ss[r + stp] - ss[r], sq[r + stp] - sq[r]);
+          d3 = fmaf(phibar, ss[r + 2 * stp] - ss[r + stp], sq[r + 2 * stp] - sq[r + stp]);
+          eps = st.eps_P;
+        } else {
+          const float *Q = (fld == 1) ? S.E : (stp == 1 ? S.F : S.G);
+          d0 = Q[r - stp] - Q[r - 2 * stp];
+          d1 = Q[r] - Q[r - stp];
+          d2 = Q[r + stp] - Q[r];
+          d3 = Q[r + 2 * stp] - Q[r + stp];
+          eps = (fld == 1) ? st.eps_E : st.eps_F;
+        }
+        weno_d(d0, d1, d2, d3, eps, Dp, Dm);
+      }
+      if (rem < NCX) {
+        S.Dx[2 * fld][rem] = Dp;
+        S.Dx[2 * fld + 1][rem] = Dm;
+      } else {
+        S.Dy[2 * fld][rem - NCX] = Dp;
+        S.Dy[2 * fld + 1][rem - NCX] = Dm;
+      }
+    }
+    __syncthreads();
+
+    // ---- phase 3: Rusanov face values relative to the left / lower cell --------
+    for (int t = tid; t < NFX + NFY; t += NT) {
+      if (t < NFX) {
+        const int fi = t % (TX + 1), lj = t / (TX + 1);
+        const int r = (lj + 3) * RX + fi + 2;  // cell f; f+1 at r+1
+        const int cl = lj * (TX + 2) + fi, cr = cl + 1;
+        const float dF = S.F[r + 1] - S.F[r];
+        const float dE = S.E[r + 1] - S.E[r];
+        const float dP = fmaf(phibar, S.s[r + 1] - S.s[r], S.q[r + 1] - S.q[r]);
+        const float uB = 0.5f * (S.uC[r] + S.uC[r + 1]);
+        const float pB = 0.5f * (S.phit[r] + S.phit[r + 1]);
+        const float lam = fabsf(uB) + sqrtf(fmaxf(0.5f * (S.ig11[r] + S.ig11[r + 1]) * pB, 0.f));
+        S.gx[0][t] = 0.5f * (dF + S.Dx[0][cl] + S.Dx[1][cr] - lam * (dP + S.Dx[5][cr] - S.Dx[4][cl]));
+        S.gx[1][t] = 0.5f * (dE + S.Dx[2][cl] + S.Dx[3][cr]);
+      } else {
+        const int yf = t - NFX;
+        const int li = yf % TX, fj = yf / TX;
+        const int r = (fj + 2) * RX + li + 3;  // cell g; g+1 at r+RX
+        const int cl = fj * TX + li, cr = cl + TX;
+        const float dG = S.G[r + RX] - S.G[r];
+        const float dE = S.E[r + RX] - S.E[r];
+        const float dP = fmaf(phibar, S.s[r + RX] - S.s[r], S.q[r + RX] - S.q[r]);
+        const float vB = 0.5f * (S.vC[r] + S.vC[r + RX]);
+        const float pB = 0.5f * (S.phit[r] + S.phit[r + RX]);
+        const float lam = fabsf(vB) + sqrtf(fmaxf(0.5f * (S.ig22[r] + S.ig22[r + RX]) * pB, 0.f));
+        S.gy[0][yf] = 0.5f * (dG + S.Dy[0][cl] + S.Dy[1][cr] - lam * (dP + S.Dy[5][cr] - S.Dy[4][cl]));
+        S.gy[1][yf] = 0.5f * (dE + S.Dy[2][cl] + S.Dy[3][cr]);
+      }
+    }
+    __syncthreads();
+
+    // ---- phase 4: tendencies, stage update, ghost push -------------------------
+    for (int t = tid; t < TX * TY; t += NT) {
+      const int li = t % TX, lj = t / TX;
+      const int i = i0 + li, j = j0 + lj;
+      if (i > N || j > N) continue;
+      const int r = (lj + 3) * RX + li + 3;
+      const int xl = lj * (TX + 1) + li, yb = lj * TX + li;
+      const float divx = (S.gx[0][xl + 1] - S.gx[0][xl] + (S.F[r] - S.F[r - 1])) * st.rdx;
+      const float dEdx = (S.gx[1][xl + 1] - S.gx[1][xl] + (S.E[r] - S.E[r - 1])) * st.rdx;
+      const float divy = (S.gy[0][yb + TX] - S.gy[0][yb] + (S.G[r] - S.G[r - RX])) * st.rdy;
+      const float dEdy = (S.gy[1][yb + TX] - S.gy[1][yb] + (S.E[r] - S.E[r - RX])) * st.rdy;
+      const float *vv = S.v + r, *uu = S.u + r;
+      const float dvdx = (-vv[-3] + 9.f * vv[-2] - 45.f * vv[-1] + 45.f * vv[1] - 9.f * vv[2] + vv[3]) * st.rdx60;
+      const float dudy = (-uu[-3 * RX] + 9.f * uu[-2 * RX] - 45.f * uu[-RX] + 45.f * uu[RX] - 9.f * uu[2 * RX] +
+                          uu[3 * RX]) *
+                         st.rdy60;
+      const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
+      const float vort = dvdx - dudy + st.m.fs[c];
+      const float tp = -(divx + divy) * st.m.inv_s[cs];
+      const float tu = fmaf(vort, S.vC[r], -dEdx * st.inv_a2);
+      const float tv = fmaf(-vort, S.uC[r], -dEdy * st.inv_a2);
+      if (st.kind == K_TEND) {
+        st.thp[c] = tp;
+        st.tu[c] = tu;
+        st.tv[c] = tv;
+        continue;
+      }
+      const float y0p = st.y0hp[c], y0u = st.y0u[c], y0v = st.y0v[c];
+      float ip, iu, iv;  // increments to Y0
+      bool fin = false;
+      switch (st.kind) {
+        case K_RK4_1:
+          st.acchp[c] = tp; st.accu[c] = tu; st.accv[c] = tv;
+          ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
+          break;
+        case K_RK4_2: {
+          st.acchp[c] = fmaf(2.f, tp, st.acchp[c]);
+          st.accu[c] = fmaf(2.f, tu, st.accu[c]);
+          st.accv[c] = fmaf(2.f, tv, st.accv[c]);
+          ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
+          break;
+        }
+        case K_RK4_4: {
+          const float k6 = st.c1 * (1.f / 6.f);
+          ip = k6 * (st.acchp[c] + tp); iu = k6 * (st.accu[c] + tu); iv = k6 * (st.accv[c] + tv);
+          fin = true;
+          break;
+        }
+        case K_RK3_1:
+          ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
+          break;
+        case K_RK3_2:
+          ip = fmaf(0.25f, st.in.hp[c] - y0p, st.c1 * tp);
+          iu = fmaf(0.25f, S.u[r] - y0u, st.c1 * tu);
+          iv = fmaf(0.25f, S.v[r] - y0v, st.c1 * tv);
+          break;
+        default:  // K_RK3_3
+          ip = fmaf(2.f / 3.f, st.in.hp[c] - y0p, st.c1 * tp);
+          iu = fmaf(2.f / 3.f, S.u[r] - y0u, st.c1 * tu);
+          iv = fmaf(2.f / 3.f, S.v[r] - y0v, st.c1 * tv);
+          fin = true;
+          break;
+      }
+      float np, nu, nv;
+      if (fin) {
+        // compensated update of the step-to-step state (TwoSum)
+        float lo[3] = {st.lohp[c], st.lou[c], st.lov[c]};
+        const float hi[3] = {y0p, y0u, y0v};
+        const float inc[3] = {ip, iu, iv};
+        float out[3];
+        for (int k = 0; k < 3; k++) {
+          const float y = inc[k] + lo[k];
+          const float tt = hi[k] + y;
+          const float bp = tt - hi[k];
+          lo[k] = (hi[k] - (tt - bp)) + (y - bp);
+          out[k] = tt;
+        }
+        np = out[0]; nu = out[1]; nv = out[2];
+        st.lohp[c] = lo[0]; st.lou[c] = lo[1]; st.lov[c] = lo[2];
+      } else {
+        np = y0p + ip; nu = y0u + iu; nv = y0v + iv;
+      }
+      st.out.hp[c] = np;
+      st.out.u[c] = nu;
+      st.out.v[c] = nv;
+      // ghost push: hp copies; the covariant wind crosses the edge through the
+      // FP64 2x2 transform G_h IA_h A_s IG_s of the receiving halo cell
+      const int h = L.h;
+      for (int side = 0; side < 4; side++) {
+        int k, m;
+        if (side == 0) { k = i; m = j; }
+        else if (side == 1) { k = N + 1 - i; m = j; }
+        else if (side == 2) { k = j; m = i; }
+        else { k = N + 1 - j; m = i; }
+        if (k > h) continue;
+        const int64_t e = ((int64_t)p * 4 + side) * h * N + (int64_t)(k - 1) * N + (m - 1);
+        const int64_t d = st.m.push[e];
+        const double *T = st.m.xf + 4 * e;
+        const double ud = T[0] * (double)nu + T[1] * (double)nv;
+        const double vd = T[2] * (double)nu + T[3] * (double)nv;
+        st.out.hp[d] = np;
+        st.out.u[d] = (float)ud;
+        st.out.v[d] = (float)vd;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---- import / export between the reference FP64 layout and the lane state ----
+__global__ void mixed_import_kernel(Layout L, const double *__restrict__ phi, const double *__restrict__ u,
+                                    const double *__restrict__ v, double phibar, double inv_a2, StateMixed out,
+                                    float *lohp, float *lou, float *lov) {
+  const int nh = L.nh;
+  const int64_t n = (int64_t)nh * nh * 6;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int ia = (int)(q % nh), ja = (int)((q / nh) % nh), p = (int)(q / ((int64_t)nh * nh));
+    const int i = ia + 1 - L.h, j = ja + 1 - L.h;
+    const int64_t c = L.idx(i, j, p);
+    if ((i < 1 || i > L.N) && (j < 1 || j > L.N)) continue;
+    const double hp = phi[q] - phibar, uu = u[q] * inv_a2, vv = v[q] * inv_a2;
+    const float fh = (float)hp, fu = (float)uu, fv = (float)vv;
+    out.hp[c] = fh;
+    out.u[c] = fu;
+    out.v[c] = fv;
+    const bool interior = i >= 1 && i <= L.N && j >= 1 && j <= L.N;
+    lohp[c] = interior ? (float)(hp - (double)fh) : 0.f;
+    lou[c] = interior ? (float)(uu - (double)fu) : 0.f;
+    lov[c] = interior ? (float)(vv - (double)fv) : 0.f;
+  }
+}
+
+__global__ void mixed_export_kernel(Layout L, StateMixed st, const float *__restrict__ lohp,
+                                    const float *__restrict__ lou, const float *__restrict__ lov, MeshF64 m,
+                                    double phibar, double a2, double *phiG, double *u, double *v, double *phi,
+                                    double *uC, double *vC, double *zonal, double *merid) {
+  const int nh = L.nh;
+  const int64_t n = (int64_t)nh * nh * 6;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int ia = (int)(q % nh), ja = (int)((q / nh) % nh), p = (int)(q / ((int64_t)nh * nh));
+    const int i = ia + 1 - L.h, j = ja + 1 - L.h;
+    const int64_t c = L.idx(i, j, p);
+    if ((i < 1 || i > L.N) && (j < 1 || j > L.N)) continue;
+    const bool interior = i >= 1 && i <= L.N && j >= 1 && j <= L.N;
+    double hp = st.hp[c], uu = st.u[c], vv = st.v[c];
+    if (interior) {
+      hp += (double)lohp[c];
+      uu += (double)lou[c];
+      vv += (double)lov[c];
+    }
+    const double ph = phibar + hp, cu = uu * a2, cv = vv * a2;
+    phi[q] = ph;
+    phiG[q] = ph * m.sqrtG[c];
+    u[q] = cu;
+    v[q] = cv;
+    uC[q] = m.ig11[c] * cu + m.ig12[c] * cv;
+    vC[q] = m.ig21[c] * cu + m.ig22[c] * cv;
+    zonal[q] = m.aig11[c] * cu + m.aig12[c] * cv;
+    merid[q] = m.aig21[c] * cu + m.aig22[c] * cv;
+  }
+}
+
+__global__ void mixed_tend_export_kernel(Layout L, const float *__restrict__ thp, const float *__restrict__ tu,
+                                         const float *__restrict__ tv, MeshF64 m, double a2, double *op,
+                                         double *ou, double *ov) {
+  const int nh = L.nh;
+  const int64_t n = (int64_t)nh * nh * 6;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int ia = (int)(q % nh), ja = (int)((q / nh) % nh), p = (int)(q / ((int64_t)nh * nh));
+    const int i = ia + 1 - L.h, j = ja + 1 - L.h;
+    const bool interior = i >= 1 && i <= L.N && j >= 1 && j <= L.N;
+    if (!interior) {
+      op[q] = 0.; ou[q] = 0.; ov[q] = 0.;
+      continue;
+    }
+    const int64_t c = L.idx(i, j, p);
+    op[q] = (double)thp[c] * m.sqrtG[c];
+    ou[q] = (double)tu[c] * a2;
+    ov[q] = (double)tv[c] * a2;
+  }
+}
+
+// FP64 mass / energy of the mixed state (diag_mod.F90:10-53), block partials.
+__global__ void mixed_diag_kernel(Layout L, StateMixed st, const float *__restrict__ lohp,
+                                  const float *__restrict__ lou, const float *__restrict__ lov, MeshF64 m,
+                                  double phibar, double a2, double *partials) {
+  __shared__ double sm[2][256];
+  const int64_t ncell = (int64_t)L.N * L.N * 6;
+  const int64_t per = (ncell + gridDim.x - 1) / gridDim.x;
+  const int64_t beg = blockIdx.x * per;
+  int64_t end = beg + per;
+  if (end > ncell) end = ncell;
+  double ms = 0., en = 0.;
+  for (int64_t q = beg + threadIdx.x; q < end; q += blockDim.x) {
+    const int i = 1 + (int)(q % L.N), j = 1 + (int)((q / L.N) % L.N), p = (int)(q / ((int64_t)L.N * L.N));
+    const int64_t c = L.idx(i, j, p);
+    const double ph = phibar + ((double)st.hp[c] + (double)lohp[c]);
+    const double cu = ((double)st.u[c] + (double)lou[c]) * a2, cv = ((double)st.v[c] + (double)lov[c]) * a2;
+    const double uc = m.ig11[c] * cu + m.ig12[c] * cv, vc = m.ig21[c] * cu + m.ig22[c] * cv;
+    const double sg = m.sqrtG[c];
+    ms += ph * sg;
+    const double t = ph + m.phis[c];
+    en += sg * (0.5 * ph * (cu * uc + cv * vc) + 0.5 * (t * t));
+  }
+  sm[0][threadIdx.x] = ms;
+  sm[1][threadIdx.x] = en;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sm[0][threadIdx.x] += sm[0][threadIdx.x + s];
+      sm[1][threadIdx.x] += sm[1][threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = sm[0][0];
+    partials[2 * blockIdx.x + 1] = sm[1][0];
+  }
+}
+
+}  // namespace
+
+int mixed_smem_bytes() { return (int)sizeof(SmemMx); }
+
+int mixed_max_grid(int device) {
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaFuncSetAttribute(mixed_stage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mixed_smem_bytes());
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel, NT, mixed_smem_bytes());
+  if (per < 1) per = 1;
+  return sms * per;
+}
+
+cudaError_t launch_mixed_stage(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid,
+                               cudaStream_t s) {
+  if (grid > nwork) grid = nwork;
+  if (grid < 1) return cudaSuccess;
+  mixed_stage_kernel<<<grid, NT, mixed_smem_bytes(), s>>>(d_stages, d_work, nwork);
+  return cudaGetLastError();
+}
+
+static int ew_grid(const Layout &L) {
+  const int64_t n = (int64_t)L.nh * L.nh * 6;
+  int64_t g = (n + 255) / 256;
+  if (g > 4096) g = 4096;
+  return (int)g;
+}
+
+cudaError_t launch_mixed_import(const Layout &L, const double *phi, const double *u, const double *v,
+                                double phibar, double inv_a2, StateMixed out, float *lohp, float *lou,
+                                float *lov, cudaStream_t s) {
+  mixed_import_kernel<<<ew_grid(L), 256, 0, s>>>(L, phi, u, v, phibar, inv_a2, out, lohp, lou, lov);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_export(const Layout &L, StateMixed st, const float *lohp, const float *lou,
+                                const float *lov, const MeshF64 &m, double phibar, double a2, double *const out[8],
+                                cudaStream_t s) {
+  mixed_export_kernel<<<ew_grid(L), 256, 0, s>>>(L, st, lohp, lou, lov, m, phibar, a2, out[0], out[1], out[2],
+                                                  out[3], out[4], out[5], out[6], out[7]);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_tend_export(const Layout &L, const float *thp, const float *tu, const float *tv,
+                                     const MeshF64 &m, double a2, double *op, double *ou, double *ov,
+                                     cudaStream_t s) {
+  mixed_tend_export_kernel<<<ew_grid(L), 256, 0, s>>>(L, thp, tu, tv, m, a2, op, ou, ov);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp, const float *lou,
+                              const float *lov, const MeshF64 &m, double phibar, double a2, double *partials,
+                              int nblocks, cudaStream_t s) {
+  mixed_diag_kernel<<<nblocks, 256, 0, s>>>(L, st, lohp, lou, lov, m, phibar, a2, partials);
+  return cudaGetLastError();
+}
+
+}  // namespace ccs

@@ -1,0 +1,253 @@
+"""Host-side API over the C ABI: mesh, initial state and the GPU step.
+
+Mirrors the reference driver (dynamic_core/src/ccsm.F90): ``Mesh`` stands for
+read_mesh (io_mod.F90:15-307) on the arrays of the host mesh generator, ``State``
+for stat_field (stat_mod.F90:7-17), ``initial_state`` for initTestCase
+(test_case_mod.F90:13-58) and ``Stepper`` for the time loop body
+(RK4 / RK3_TVD + copyStat, ccsm.F90:50-67).  All arrays are numpy float64 in the
+reference's Fortran order, flattened: cell fields are (N+2h, N+2h, 6).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+PI = np.pi
+D2R = PI / 180.0
+
+# BASELINE constants (the reference hard-codes radius 6371229 in constants_mod.F90:9)
+RADIUS = 6.371e6
+GRAVITY = 9.80616
+OMEGA = 7.292e-5
+
+STATE_FIELDS = L.STATE_FIELDS
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Mesh:
+    """Metric arrays of an N x N x 6 cubed sphere with `halo` ghost cells."""
+
+    def __init__(self, N: int, halo: int = 3, radius: float = RADIUS, omega: float = OMEGA,
+                 gravity: float = GRAVITY, phis: np.ndarray | None = None):
+        self.N, self.halo = int(N), int(halo)
+        self.radius, self.omega, self.gravity = float(radius), float(omega), float(gravity)
+        self.nh = self.N + 2 * self.halo
+        self.ncell = self.nh * self.nh * 6
+        lib = L.lib()
+        n = self.N * self.N * 6
+        self.file = {k: np.zeros(n) for k in ("lon", "lat", "x", "y", "z")}
+        self.file["jab"] = np.zeros(6 * n)
+        f = self.file
+        L.check(lib.ccs_mesh_generate(self.N, L.CCS_MAP_GNOMONIC_EQUIANGULAR, _ptr(f["lon"]), _ptr(f["lat"]),
+                                      _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"])),
+                "ccs_mesh_generate")
+        nc = self.ncell
+        self.sqrtG = np.zeros(nc)
+        self.matrixG = np.zeros(4 * nc)
+        self.matrixIG = np.zeros(4 * nc)
+        self.matrixA = np.zeros(4 * nc)
+        self.matrixIA = np.zeros(4 * nc)
+        self.f = np.zeros(nc)
+        self.lon = np.zeros(nc)
+        self.lat = np.zeros(nc)
+        self.sinlat = np.zeros(nc)
+        self.coslat = np.zeros(nc)
+        L.check(lib.ccs_mesh_derive(self.N, self.halo, self.radius, self.omega, _ptr(f["lon"]), _ptr(f["lat"]),
+                                    _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"]), _ptr(self.sqrtG),
+                                    _ptr(self.matrixG), _ptr(self.matrixIG), _ptr(self.matrixA),
+                                    _ptr(self.matrixIA), _ptr(self.f), _ptr(self.lon), _ptr(self.lat),
+                                    _ptr(self.sinlat), _ptr(self.coslat)), "ccs_mesh_derive")
+        # dx = dy = (90/N) degrees in radians, as io_mod.F90:54-55 converts them
+        self.dx = (90.0 / self.N) * D2R
+        self.dy = self.dx
+        self.phis = np.zeros(nc) if phis is None else np.ascontiguousarray(phis, dtype=np.float64)
+
+    def view(self) -> L.MeshView:
+        mv = L.MeshView()
+        for name in ("sqrtG", "matrixG", "matrixIG", "matrixA", "matrixIA", "f", "phis"):
+            setattr(mv, name, _ptr(getattr(self, name)))
+        return mv
+
+    def field(self, a: np.ndarray) -> np.ndarray:
+        """(i, j, panel) view of a flattened cell field."""
+        return a.reshape((self.nh, self.nh, 6), order="F")
+
+    def interior_mask(self) -> np.ndarray:
+        m = np.zeros((self.nh, self.nh, 6), dtype=bool, order="F")
+        h, N = self.halo, self.N
+        m[h:h + N, h:h + N, :] = True
+        return m.reshape(-1, order="F")
+
+    def corner_mask(self) -> np.ndarray:
+        """True on the never-filled h x h corner blocks."""
+        idx = np.arange(self.nh) - self.halo + 1
+        out_i = (idx < 1) | (idx > self.N)
+        c = out_i[:, None] & out_i[None, :]
+        return np.repeat(c[:, :, None], 6, axis=2).reshape(-1, order="F")
+
+
+@dataclass
+class State:
+    """stat_field: nine (N+2h)^2 x 6 arrays."""
+    arrays: dict = field(default_factory=dict)
+
+    @classmethod
+    def zeros(cls, mesh: Mesh) -> "State":
+        return cls({k: np.zeros(mesh.ncell) for k in STATE_FIELDS})
+
+    def __getitem__(self, k):
+        return self.arrays[k]
+
+    def __setitem__(self, k, v):
+        self.arrays[k] = v
+
+    def copy(self) -> "State":
+        return State({k: v.copy() for k, v in self.arrays.items()})
+
+    def view(self, fields=STATE_FIELDS) -> L.StateView:
+        sv = L.StateView()
+        for k in fields:
+            setattr(sv, k, _ptr(self.arrays[k]))
+        return sv
+
+
+def initial_state(mesh: Mesh, kind: int = L.CCS_IC_SEEDED, seed: int = 1, h0: float = 8000.0,
+                  h_rms: float = 200.0, wind_max: float = 40.0, lmax_h: int = 12, lmax_psi: int = 12,
+                  lmax_oro: int = 0, oro_rms: float = 1000.0, oro_max: float = 2000.0) -> State:
+    """initTestCase equivalent: sets mesh.phis and returns stat(old)."""
+    lib = L.lib()
+    p = L.ICParams(kind=kind, lmax_h=lmax_h, lmax_psi=lmax_psi, lmax_oro=lmax_oro, seed=seed, h0=h0,
+                   h_rms=h_rms, wind_max=wind_max, oro_rms=oro_rms, oro_max=oro_max)
+    s = State.zeros(mesh)
+    L.check(lib.ccs_initial_condition(mesh.N, mesh.halo, mesh.radius, mesh.gravity, mesh.omega, C.byref(p),
+                                      _ptr(mesh.lon), _ptr(mesh.lat), _ptr(mesh.sinlat), _ptr(mesh.coslat),
+                                      _ptr(s["phi"]), _ptr(s["zonal_wind"]), _ptr(s["meridional_wind"]),
+                                      _ptr(mesh.phis)), "ccs_initial_condition")
+    mv, sv = mesh.view(), s.view()
+    L.check(lib.ccs_state_from_sphere(mesh.N, mesh.halo, C.byref(mv), C.byref(sv)), "ccs_state_from_sphere")
+    return s
+
+
+def cfl_dt(mesh: Mesh, state: State, cfl: float = 0.5) -> float:
+    mv, sv = mesh.view(), state.view()
+    dt = L.lib().ccs_cfl_dt(mesh.N, mesh.halo, cfl, mesh.dx, mesh.dy, C.byref(mv), C.byref(sv))
+    if not dt > 0:
+        raise ValueError("CFL time step undefined (non-positive depth?)")
+    return dt
+
+
+def ghost_map(N: int, halo: int) -> np.ndarray:
+    nh = N + 2 * halo
+    out = np.zeros(nh * nh * 6, dtype=np.int64)
+    L.check(L.lib().ccs_ghost_map(N, halo, out.ctypes.data_as(C.POINTER(C.c_int64))), "ccs_ghost_map")
+    return out
+
+
+class Stepper:
+    """One instance of the GPU step (a ccs_handle)."""
+
+    def __init__(self, mesh: Mesh, dt: float, precision: str = "fp64", scheme: str = "RK4",
+                 e_dissipation: int = L.CCS_EDISS_ZERO, device: int = 0, phi_mean: float = 0.0,
+                 share_with: "Stepper | None" = None):
+        self.mesh = mesh
+        self.dt = float(dt)
+        cfg = L.Config(N=mesh.N, halo=mesh.halo, scheme=L.CCS_RK4 if scheme == "RK4" else L.CCS_RK3_TVD,
+                       precision=L.CCS_FP64 if precision == "fp64" else L.CCS_MIXED,
+                       e_dissipation=e_dissipation, device=device, dx=mesh.dx, dy=mesh.dy, dt=self.dt,
+                       radius=mesh.radius, gravity=mesh.gravity, omega=mesh.omega, phi_mean=phi_mean)
+        self._cfg = cfg
+        h = C.c_void_p()
+        lib = L.lib()
+        if share_with is None:
+            mv = mesh.view()
+            L.check(lib.ccs_init(C.byref(cfg), C.byref(mv), C.byref(h)), "ccs_init")
+        else:
+            L.check(lib.ccs_init_shared(C.byref(cfg), share_with.handle, C.byref(h)), "ccs_init_shared")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            L.lib().ccs_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, s: State):
+        sv = s.view()
+        L.check(L.lib().ccs_set_state(self.handle, C.byref(sv)), "ccs_set_state", self.handle)
+
+    def get_state(self, out: State | None = None) -> State:
+        out = out if out is not None else State.zeros(self.mesh)
+        sv = out.view()
+        L.check(L.lib().ccs_get_state(self.handle, C.byref(sv)), "ccs_get_state", self.handle)
+        return out
+
+    def step(self, nsteps: int = 1):
+        L.check(L.lib().ccs_step(self.handle, int(nsteps)), "ccs_step", self.handle)
+
+    def step_async(self, nsteps: int = 1):
+        L.check(L.lib().ccs_step_async(self.handle, int(nsteps)), "ccs_step_async", self.handle)
+
+    def sync(self):
+        L.check(L.lib().ccs_sync(self.handle), "ccs_sync", self.handle)
+
+    def spatial_operator(self):
+        n = self.mesh.ncell
+        t = [np.zeros(n) for _ in range(3)]
+        L.check(L.lib().ccs_spatial_operator(self.handle, _ptr(t[0]), _ptr(t[1]), _ptr(t[2])),
+                "ccs_spatial_operator", self.handle)
+        return tuple(t)
+
+    def diag(self):
+        m, e = C.c_double(), C.c_double()
+        L.check(L.lib().ccs_diag(self.handle, C.byref(m), C.byref(e)), "ccs_diag", self.handle)
+        return m.value, e.value
+
+    @property
+    def stream_ptr(self) -> int:
+        """The cudaStream_t of this handle (for torch.cuda.ExternalStream)."""
+        return L.lib().ccs_stream(self.handle) or 0
+
+    def timing(self, enable: int = -1, reset: int = 0):
+        ms, n = C.c_double(), C.c_int64()
+        L.check(L.lib().ccs_timing(self.handle, enable, reset, C.byref(ms), C.byref(n)), "ccs_timing")
+        return ms.value, n.value
+
+
+class Batch:
+    """Members advanced together: one launch per lane and RK stage."""
+
+    def __init__(self, members: list[Stepper]):
+        self.members = members
+        arr = (C.c_void_p * len(members))(*[m.handle for m in members])
+        b = C.c_void_p()
+        L.check(L.lib().ccs_batch_create(arr, len(members), C.byref(b)), "ccs_batch_create")
+        self.handle = b
+
+    def step(self, nsteps: int = 1):
+        L.check(L.lib().ccs_batch_step(self.handle, int(nsteps)), "ccs_batch_step")
+
+    def close(self):
+        if self.handle:
+            L.lib().ccs_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

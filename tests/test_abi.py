@@ -1,0 +1,106 @@
+"""The C ABI library loads and exports every declared entry point; the host-only
+entry points work without a GPU; invalid configurations are rejected before any
+device call."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conformal_cubed_sphere_gb300 import _lib as L
+from conformal_cubed_sphere_gb300 import model as M
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "ccs_gpu.h"
+
+
+def declared_functions():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(ccs_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("ccs_init", "ccs_set_state", "ccs_step", "ccs_get_state", "ccs_diag", "ccs_destroy",
+                     "ccs_strerror", "ccs_batch_create", "ccs_batch_step", "ccs_spatial_operator"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(str(L.LIB_PATH))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding covers them all
+    assert set(declared_functions()) <= set(L.SIGNATURES)
+
+
+def test_abi_version_and_strerror():
+    lib = L.lib()
+    assert lib.ccs_abi_version() == 1
+    assert lib.ccs_strerror(0) == b"ok"
+    assert lib.ccs_strerror(L.CCS_ERR_ARG) == b"invalid argument"
+
+
+def _cfg(**kw):
+    base = dict(N=8, halo=3, scheme=0, precision=0, e_dissipation=0, device=0, dx=0.1, dy=0.1, dt=10.0,
+                radius=6.371e6, gravity=9.80616, omega=7.292e-5, phi_mean=0.0)
+    base.update(kw)
+    return L.Config(**base)
+
+
+@pytest.mark.parametrize("bad", [dict(N=0), dict(halo=2), dict(scheme=7), dict(precision=3), dict(dt=-1.0),
+                                 dict(dx=float("nan")), dict(e_dissipation=5), dict(radius=0.0)])
+def test_invalid_config_rejected_without_device(bad):
+    mesh = M.Mesh(8, 3)
+    mv = mesh.view()
+    h = C.c_void_p()
+    rc = L.lib().ccs_init(C.byref(_cfg(**bad)), C.byref(mv), C.byref(h))
+    assert rc == L.CCS_ERR_ARG
+    assert not h.value
+
+
+def test_null_arguments_rejected():
+    lib = L.lib()
+    assert lib.ccs_init(None, None, None) == L.CCS_ERR_ARG
+    assert lib.ccs_step(None, 1) == L.CCS_ERR_ARG
+    assert lib.ccs_set_state(None, None) == L.CCS_ERR_ARG
+    assert lib.ccs_get_state(None, None) == L.CCS_ERR_ARG
+    assert lib.ccs_ghost_map(0, 3, None) == L.CCS_ERR_ARG
+    lib.ccs_destroy(None)
+
+
+def test_host_mesh_and_initial_state_on_cpu():
+    mesh = M.Mesh(12, 3)
+    s = M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=5, lmax_oro=8)
+    im = mesh.interior_mask()
+    h = s["phi"][im] / mesh.gravity
+    assert abs(np.sqrt(np.mean((h - 8000.0) ** 2)) - 200.0) < 1e-6
+    speed = np.hypot(s["zonal_wind"][im], s["meridional_wind"][im])
+    assert abs(speed.max() - 40.0) < 1e-9
+    hs = mesh.phis[im] / mesh.gravity
+    assert hs.min() >= 0.0 and hs.max() <= 2000.0 and hs.max() > 0.0
+    assert M.cfl_dt(mesh, s, 0.5) > 0
+    # the same seed gives the same state; another seed does not
+    s2 = M.initial_state(M.Mesh(12, 3), kind=L.CCS_IC_SEEDED, seed=5, lmax_oro=8)
+    s3 = M.initial_state(M.Mesh(12, 3), kind=L.CCS_IC_SEEDED, seed=6, lmax_oro=8)
+    assert np.array_equal(s["phi"], s2["phi"]) and not np.array_equal(s["phi"], s3["phi"])
+
+
+def test_streamfunction_winds_are_nondivergent():
+    # divergence of the seeded wind on the sphere, by finite differences of the
+    # analytic winds along the mesh: small compared with the vorticity
+    mesh = M.Mesh(32, 3)
+    s = M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=2, lmax_oro=0)
+    F = mesh.field
+    h, N = 3, 32
+    sg = F(mesh.sqrtG)
+    uC = F(s["uC"])
+    vC = F(s["vC"])
+    div = ((sg * uC)[h + 1:h + N + 1, h:h + N] - (sg * uC)[h - 1:h + N - 1, h:h + N]) / (2 * mesh.dx) + \
+          ((sg * vC)[h:h + N, h + 1:h + N + 1] - (sg * vC)[h:h + N, h - 1:h + N - 1]) / (2 * mesh.dy)
+    u = F(s["u"])
+    v = F(s["v"])
+    vort = (v[h + 1:h + N + 1, h:h + N] - v[h - 1:h + N - 1, h:h + N]) / (2 * mesh.dx) - \
+           (u[h:h + N, h + 1:h + N + 1] - u[h:h + N, h - 1:h + N - 1]) / (2 * mesh.dy)
+    inner = (slice(4, N - 4), slice(4, N - 4))
+    assert np.max(np.abs(div[inner])) < 0.05 * np.max(np.abs(vort[inner]))

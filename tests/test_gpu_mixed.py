@@ -1,0 +1,104 @@
+"""Mixed-precision lane: errors against the FP64 oracle on the same inputs,
+conservation, and batching (ensembles and uneven grids) against single runs."""
+import numpy as np
+import pytest
+
+from conformal_cubed_sphere_gb300 import _lib as L
+from conformal_cubed_sphere_gb300 import model as M
+from oracle import oracle as O
+from tests.helpers import bitwise_equal, seeded_case, valid_mask
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b, m):
+    return float(np.linalg.norm(a[m] - b[m]) / np.linalg.norm(b[m]))
+
+
+@pytest.mark.parametrize("oro", [False, True])
+def test_tendency_close_to_fp64(oro):
+    mesh, s, dt = seeded_case(32, 3, seed=3, oro=oro)
+    g = M.Stepper(mesh, dt, precision="mixed")
+    g.set_state(s)
+    o = O.Oracle.from_mesh(mesh)
+    o.set_state(s.arrays)
+    tg, to = g.spatial_operator(), o.spatial_operator()
+    im = mesh.interior_mask()
+    # tolerance: FP32 differences of O(1e4) geopotentials give ~1e-7 relative
+    # errors per face value; the tendency is a difference of faces
+    for a, b, tol in zip(tg, to, (2e-4, 2e-4, 2e-4)):
+        assert rel_l2(a, b, im) < tol
+
+
+@pytest.mark.parametrize("oro", [False, True])
+def test_100_steps_error_vs_fp64(oro):
+    mesh, s, dt = seeded_case(32, 3, seed=1, oro=oro)
+    g = M.Stepper(mesh, dt, precision="mixed")
+    g.set_state(s)
+    o = O.Oracle.from_mesh(mesh)
+    o.set_state(s.arrays)
+    g.step(100)
+    o.run(dt, 100)
+    a, b = g.get_state(), o.get_state()
+    im = mesh.interior_mask()
+    # h relative L2 (the headline error measure) and winds
+    assert rel_l2(a["phi"], b["phi"], im) < 1e-6
+    assert rel_l2(a["zonal_wind"], b["zonal_wind"], im) < 1e-4
+    assert rel_l2(a["meridional_wind"], b["meridional_wind"], im) < 1e-4
+
+
+def test_mass_drift_small():
+    mesh, s, dt = seeded_case(32, 3, seed=4, oro=True)
+    g = M.Stepper(mesh, dt, precision="mixed")
+    g.set_state(s)
+    m0, e0 = g.diag()
+    g.step(50)
+    m1, e1 = g.diag()
+    assert abs(m1 - m0) / abs(m0) < 1e-8
+
+
+def test_ensemble_batch_equals_members_alone():
+    mesh = M.Mesh(24, 3)
+    states = [M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=100 + k, h_rms=150 + 25 * k,
+                              wind_max=30 + 5 * k) for k in range(4)]
+    dt = min(M.cfl_dt(mesh, st, 0.5) for st in states)
+    owner = M.Stepper(mesh, dt, precision="mixed", phi_mean=8000 * 9.80616)
+    members = [owner] + [M.Stepper(mesh, dt, precision="mixed", share_with=owner, phi_mean=8000 * 9.80616)
+                         for _ in range(3)]
+    for st, m in zip(states, members):
+        m.set_state(st)
+    b = M.Batch(members)
+    b.step(4)
+    msk = valid_mask(mesh)
+    for st, m in zip(states, members):
+        alone = M.Stepper(mesh, dt, precision="mixed", phi_mean=8000 * 9.80616)
+        alone.set_state(st)
+        alone.step(4)
+        x, y = m.get_state(), alone.get_state()
+        for k in ("phiG", "u", "v", "phi"):
+            assert bitwise_equal(x[k], y[k], msk), k
+
+
+def test_uneven_batch_mixed_lanes():
+    """Different resolutions, time steps and lanes in one batch: each member's
+    result equals its single run bit for bit."""
+    specs = [(16, "mixed"), (24, "fp64"), (12, "mixed"), (20, "fp64")]
+    members, ref = [], []
+    for k, (N, lane) in enumerate(specs):
+        mesh = M.Mesh(N, 3)
+        st = M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=40 + k, lmax_oro=8)
+        dt = M.cfl_dt(mesh, st, 0.5)
+        a = M.Stepper(mesh, dt, precision=lane)
+        a.set_state(st)
+        members.append(a)
+        b = M.Stepper(mesh, dt, precision=lane)
+        b.set_state(st)
+        ref.append(b)
+    batch = M.Batch(members)
+    batch.step(3)
+    for a, b in zip(members, ref):
+        b.step(3)
+        x, y = a.get_state(), b.get_state()
+        msk = valid_mask(a.mesh)
+        for k in ("phiG", "u", "v"):
+            assert bitwise_equal(x[k], y[k], msk), k

@@ -1,0 +1,204 @@
+"""Known-answer tests pinning the CPU oracle against the reference source.
+
+The reference ships no tests or golden vectors and cannot be compiled here (no
+Fortran compiler), so these checks restate behaviour the Fortran source implies:
+WENO exactness on polynomials, the ghost-fill permutation, the metric
+derivation, projection round trips, the steady interior of test case 2 and the
+sphere-area check of io_mod.F90:306.
+"""
+import numpy as np
+import pytest
+
+from conformal_cubed_sphere_gb300 import _lib as L
+from conformal_cubed_sphere_gb300 import model as M
+from oracle import oracle as O
+from tests.helpers import seeded_case
+
+
+# ---- WENO_limiter (spatial_operators_mod.F90:282-361) -------------------------
+
+@pytest.mark.parametrize("c", [0.0, 1.0, -3.5, 1e18])
+def test_weno_constant_is_reproduced(c):
+    # the candidate stencils sum to one: constant data comes back to within rounding
+    for d in (1, -1):
+        assert O.weno_limiter([c] * 5, d) == pytest.approx(c, rel=4e-16, abs=0)
+
+
+@pytest.mark.parametrize("a,b", [(1.0, 0.5), (-2.0, 3.0), (1e3, 1e-3)])
+def test_weno_linear_reconstructs_face_value(a, b):
+    # cell averages of a + b x on unit cells centred at -2..2; face at x = +1/2 ("+")
+    # and x = -1/2 ("-" reconstructs the left face of the centre cell)
+    Q = [a + b * x for x in (-2, -1, 0, 1, 2)]
+    assert O.weno_limiter(Q, 1) == pytest.approx(a + 0.5 * b, rel=1e-13, abs=1e-12)
+    assert O.weno_limiter(Q, -1) == pytest.approx(a - 0.5 * b, rel=1e-13, abs=1e-12)
+
+
+def test_weno_mirror_symmetry():
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        Q = rng.normal(size=5)
+        assert O.weno_limiter(Q, -1) == pytest.approx(O.weno_limiter(Q[::-1], 1), rel=1e-12, abs=1e-14)
+
+
+def test_weno_smooth_data_fifth_order():
+    # WENO-Z on smooth data converges at 5th order to the point value at the face
+    errs = []
+    for n in (40, 80):
+        h = 1.0 / n
+        x = np.arange(-2, 3) * h
+        cell_avg = (np.sin(x + h / 2) - np.sin(x - h / 2)) / h  # averages of cos
+        errs.append(abs(O.weno_limiter(cell_avg, 1) - np.cos(h / 2)))
+    assert errs[0] / errs[1] > 16  # at least 4th order; 5th asymptotically
+
+
+def test_weno_branch_switches():
+    # tau40 <= min(beta) and tau41 > min(beta): omega = [1/3, 2/3, 0]
+    Q = np.array([0.0, 0.0, 0.0, 1.0, 1.0])
+    b1 = 0.0
+    st = [Q[0] / 3 - 7 / 6 * Q[1] + 11 / 6 * Q[2], -Q[1] / 6 + 5 / 6 * Q[2] + Q[3] / 3,
+          Q[2] / 3 + 5 / 6 * Q[3] - Q[4] / 6]
+    beta = [13 / 12 * (Q[0] - 2 * Q[1] + Q[2]) ** 2 + 0.25 * (Q[0] - 4 * Q[1] + 3 * Q[2]) ** 2,
+            13 / 12 * (Q[1] - 2 * Q[2] + Q[3]) ** 2 + 0.25 * (Q[1] - Q[3]) ** 2,
+            13 / 12 * (Q[2] - 2 * Q[3] + Q[4]) ** 2 + 0.25 * (3 * Q[2] - 4 * Q[3] + Q[4]) ** 2]
+    assert beta[0] == b1
+    t40, t41 = abs(beta[0] - beta[1]), abs(beta[1] - beta[2])
+    assert not (t40 <= min(beta) and t41 > min(beta))  # this data takes the WENO-Z branch
+    w = np.array([0.1, 0.6, 0.3]) * (1 + abs(beta[2] - beta[0]) / (1e-2 + np.array(beta)))
+    expect = np.dot(st, w / w.sum())
+    assert O.weno_limiter(Q, 1) == pytest.approx(expect, rel=1e-14)
+
+
+# ---- ghost fill (ghost_mod.f90:18-82) ------------------------------------------
+
+@pytest.mark.parametrize("N,h", [(4, 3), (8, 3), (12, 4), (16, 3)])
+def test_ghost_map_equals_fill_halo(N, h):
+    mesh = M.Mesh(N, h)
+    idx = np.arange(mesh.ncell, dtype=np.float64)
+    filled = O.fill_halo(N, h, np.where(mesh.interior_mask(), idx, -1.0))
+    gm = M.ghost_map(N, h)
+    cm = mesh.corner_mask()
+    assert np.array_equal(gm[~cm], filled[~cm].astype(np.int64))
+    assert np.all(gm[cm] == -1)
+    # every halo edge cell is a copy of an interior cell; interior cells map to themselves
+    assert np.array_equal(gm[mesh.interior_mask()], np.flatnonzero(mesh.interior_mask()))
+
+
+def test_halo_cells_are_geometric_neighbours():
+    N, h = 16, 3
+    mesh = M.Mesh(N, h)
+    x = O.fill_halo(N, h, _cart(mesh, 0))
+    y = O.fill_halo(N, h, _cart(mesh, 1))
+    z = O.fill_halo(N, h, _cart(mesh, 2))
+    F = mesh.field
+    X, Y, Z = F(x), F(y), F(z)
+    ang = np.pi / 2 / N
+    for p in range(6):
+        for k in range(h):
+            # distance between consecutive cells across the left and right edges
+            a = np.stack([X[h - k, h:h + N, p], Y[h - k, h:h + N, p], Z[h - k, h:h + N, p]])
+            b = np.stack([X[h - k - 1, h:h + N, p], Y[h - k - 1, h:h + N, p], Z[h - k - 1, h:h + N, p]])
+            d = np.arccos(np.clip(np.sum(a * b, axis=0), -1, 1))
+            assert np.all(d < 1.6 * ang) and np.all(d > 0.5 * ang)
+
+
+def _cart(mesh, comp):
+    N, h = mesh.N, mesh.halo
+    out = np.zeros(mesh.ncell)
+    F = mesh.field(out)
+    f = mesh.file[("x", "y", "z")[comp]].reshape((N, N, 6), order="F")
+    F[h:h + N, h:h + N, :] = f
+    return out
+
+
+# ---- metric derivation (io_mod.F90:119-220, 295-306) -----------------------------
+
+@pytest.mark.parametrize("N,h", [(8, 3), (20, 4)])
+def test_metric_derivation_matches_oracle_bitwise(N, h):
+    mesh = M.Mesh(N, h)
+    f = mesh.file
+    d = O.derive_metrics(N, h, mesh.radius, mesh.omega, f["lon"], f["lat"], f["x"], f["y"], f["z"], f["jab"])
+    for k in ("sqrtG", "matrixG", "matrixIG", "matrixA", "matrixIA", "f", "lon", "lat", "sinlat", "coslat"):
+        assert np.array_equal(d[k], getattr(mesh, k)), k
+
+
+def test_jab_fill_matches_halo_metric_continuity():
+    # FillJab re-expresses the neighbour's Jacobian in this panel's axes: the halo
+    # cell's sqrtG equals its source cell's sqrtG exactly (a signed permutation of
+    # the columns leaves det(J^T J) unchanged)
+    N, h = 12, 3
+    mesh = M.Mesh(N, h)
+    gm = M.ghost_map(N, h)
+    halo = (~mesh.interior_mask()) & (~mesh.corner_mask())
+    assert np.allclose(mesh.sqrtG[halo], mesh.sqrtG[gm[halo]], rtol=1e-14, atol=0)
+
+
+def test_sphere_area():
+    for N in (16, 48):
+        mesh = M.Mesh(N, 3)
+        area = np.sum(mesh.sqrtG[mesh.interior_mask()]) * mesh.dx * mesh.dy
+        assert abs(area / (4 * np.pi * mesh.radius ** 2) - 1) < 2e-3 * (16 / N) ** 2
+
+
+def test_projection_round_trip():
+    # covProjSphere2Plane(covProjPlane2Sphere(u)) = u (projection_mod.F90:60-96)
+    mesh = M.Mesh(10, 3)
+    m = ~mesh.corner_mask()
+    G = mesh.matrixG.reshape(-1, 2, 2).transpose(0, 2, 1)
+    IG = mesh.matrixIG.reshape(-1, 2, 2).transpose(0, 2, 1)
+    A = mesh.matrixA.reshape(-1, 2, 2).transpose(0, 2, 1)
+    IA = mesh.matrixIA.reshape(-1, 2, 2).transpose(0, 2, 1)
+    R = np.einsum("nij,njk,nkl,nlm->nim", G, IA, A, IG)[m]
+    assert np.allclose(R, np.eye(2)[None], atol=1e-12)
+
+
+# ---- the step ------------------------------------------------------------------
+
+def test_case2_interior_tendency_converges():
+    """Test case 2 is an exact steady state of the continuous equations
+    (test_case_mod.F90:61-95): away from panel edges the discrete tendency is pure
+    truncation error and falls at high order with resolution."""
+    errs = []
+    for N in (24, 48):
+        h = 3
+        mesh = M.Mesh(N, h)
+        s = M.initial_state(mesh, kind=L.CCS_IC_CASE2)
+        orc = O.Oracle.from_mesh(mesh)
+        orc.set_state(s.arrays)
+        tp, tu, tv = orc.spatial_operator()
+        F = mesh.field
+        q = N // 4  # the central half of each panel
+        inner = (slice(h + q, h + N - q), slice(h + q, h + N - q), slice(None))
+        errs.append(np.max(np.abs(F(tp)[inner] / F(s["phiG"])[inner])))
+    # cell-centre point values fed to a cell-average reconstruction: third order
+    assert errs[0] / errs[1] > 6
+    assert errs[1] < 1e-9
+
+
+def test_oracle_mass_conserved_and_deterministic():
+    mesh, s, dt = seeded_case(12, oro=True)
+    a = O.Oracle.from_mesh(mesh)
+    a.set_state(s.arrays)
+    m0 = a.total_mass()
+    a.run(dt, 5)
+    assert abs(a.total_mass() - m0) / abs(m0) < 1e-12
+    b = O.Oracle.from_mesh(mesh)
+    b.set_state(s.arrays)
+    b.run(dt, 5)
+    sa, sb = a.get_state(), b.get_state()
+    for k in ("phiG", "u", "v"):
+        assert np.array_equal(sa[k], sb[k])
+
+
+def test_rk4_combination_matches_four_stage_formula():
+    """phiG(new) = phiG(old) + dt (((k1 + 2k2) + 2k3) + k4) / 6 on the interior,
+    bit for bit (time_scheme_mod.F90:13-44; the boundary correction leaves interior
+    phiG untouched)."""
+    mesh, s, dt = seeded_case(8, oro=False)
+    o = O.Oracle.from_mesh(mesh)
+    o.set_state(s.arrays)
+    o.rk4_once(dt)
+    new = o.get_state(slot=1)
+    k = [o.get_tend(slot)[0] for slot in (-1, -2, -3, -4)]
+    im = mesh.interior_mask()
+    comb = (k[0] + 2.0 * k[1] + 2.0 * k[2] + k[3]) / 6.0
+    assert np.array_equal(new["phiG"][im], (s["phiG"] + dt * comb)[im])
