@@ -27,6 +27,7 @@ CCS_MIXED = 1
 CCS_EDISS_ZERO = 0
 CCS_EDISS_RECONSTRUCT = 1
 CCS_MAP_GNOMONIC_EQUIANGULAR = 0
+CCS_MAP_CONFORMAL = 1
 CCS_IC_CASE2 = 2
 CCS_IC_CASE5 = 5
 CCS_IC_CASE6 = 6

@@ -3,7 +3,9 @@
 // reference test cases and seeded initial states.  Runs once per run on the CPU.
 #include "ccs_internal.h"
 
+#include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -270,39 +272,315 @@ extern "C" int ccs_ghost_map(int N, int halo, int64_t *src_index) {
   return CCS_OK;
 }
 
-// Equiangular gnomonic panel map in the panel frames of cuco.f90:89-105 (rotp0).
+// ---------------------------------------------------------------------------
+// Cube-face maps in the face-local frame: face centre at (0,0,1), map coordinates
+// X, Y in [-1, 1] along the local x and y axes.  Each returns the unit-sphere
+// point and its derivatives with respect to X and Y.
+// ---------------------------------------------------------------------------
+namespace {
+
+using cd = std::complex<double>;
+
+// Equiangular gnomonic: angle coordinates (X, Y) * pi/4.
+void gnomonic_local(double X, double Y, double P[3], double dX[3], double dY[3]) {
+  const double al = X * (kPi / 4.), be = Y * (kPi / 4.);
+  const double t = std::tan(al), u = std::tan(be);
+  const double rho = std::sqrt(1. + t * t + u * u);
+  const double r3 = rho * rho * rho;
+  P[0] = t / rho; P[1] = u / rho; P[2] = 1. / rho;
+  const double ca = (kPi / 4.) * (1. + t * t), cb = (kPi / 4.) * (1. + u * u);
+  dX[0] = ca * (1. + u * u) / r3; dX[1] = -ca * t * u / r3; dX[2] = -ca * t / r3;
+  dY[0] = -cb * t * u / r3; dY[1] = cb * (1. + t * t) / r3; dY[2] = -cb * u / r3;
+}
+
+// Conformal cubic map (the map of Rancic, Purser and Mesinger 1996 that the
+// reference mesh generator evaluates with Purser's series library), built here
+// from two automorphic functions of the face's symmetry group:
+//   * the flat square S = [-1,1]^2 is tiled by the (2,4,4) reflection group whose
+//     automorphic function is J_sq(z) = (wp(z)/e1)^2 = 4 (dn/sn)^4 (K z | m=1/2),
+//     wp the Weierstrass function of the lattice 2Z + 2iZ (lemniscatic case);
+//   * the spherical face, stereographically projected from the antipode of its
+//     centre (w = (x + i y) / (1 + z)), is tiled by the octahedral (2,3,4) group
+//     whose automorphic function is Klein's J_oct(w) = P^3 / (108 w^4 (w^4-1)^4),
+//     P = w^8 + 14 w^4 + 1.
+// Both send face centre -> infinity, edge midpoint -> 1, corner -> 0 and map each
+// of the 8 symmetry triangles of a face one-to-one onto a half plane, so the
+// conformal map is w = J_oct^-1(J_sq(z)).  J_oct is inverted by Newton's method
+// with continuation along the ray from the face centre.
+
+// sn, cn, dn of a real argument u in [0, K] for parameter m (AGM, A&S 16.4); for
+// u > K/2 the quarter-period identities keep cn and dn accurate near u = K.
+struct Jac { double sn, cn, dn; };
+double agm(double a, double b) {
+  for (int it = 0; it < 64 && std::fabs(a - b) > 1e-17 * a; it++) {
+    const double an = 0.5 * (a + b);
+    b = std::sqrt(a * b);
+    a = an;
+  }
+  return 0.5 * (a + b);
+}
+Jac jac_small(double u, double m) {
+  double a[20], c[20];
+  a[0] = 1.;
+  double b = std::sqrt(1. - m);
+  c[0] = std::sqrt(m);
+  int n = 0;
+  while (std::fabs(c[n]) > 1e-18 && n < 18) {
+    const double an = 0.5 * (a[n] + b);
+    const double cn = 0.5 * (a[n] - b);
+    b = std::sqrt(a[n] * b);
+    n++;
+    a[n] = an;
+    c[n] = cn;
+  }
+  double phi = std::ldexp(a[n] * u, n);
+  for (int k = n; k >= 1; k--) phi = 0.5 * (phi + std::asin(c[k] / a[k] * std::sin(phi)));
+  Jac r;
+  r.sn = std::sin(phi);
+  r.cn = std::cos(phi);
+  r.dn = std::sqrt(1. - m * r.sn * r.sn);
+  return r;
+}
+Jac jac(double u, double m, double K) {
+  if (u <= 0.5 * K) return jac_small(u, m);
+  const Jac v = jac_small(K - u, m);  // sn(K-v) = cd v, cn(K-v) = k' sd v, dn(K-v) = k' nd v
+  const double kp = std::sqrt(1. - m);
+  return Jac{v.cn / v.dn, kp * v.sn / v.dn, kp / v.dn};
+}
+
+struct Conformal {
+  double K;   // K(m = 1/2) = K'
+  double c1;  // w ~ c1 z at the centre
+  cd wc;      // corner of the fundamental triangle, w_c^4 = -7 + 4 sqrt 3
+  Conformal() {
+    K = kPi / (2. * agm(1., std::sqrt(0.5)));
+    c1 = K / std::pow(432., 0.25);
+    wc = cd(1., 1.) / (std::sqrt(3.) + 1.);
+  }
+  // sn, dn, cn of K z for z = x + i y with 0 <= x, y <= 1 (A&S 16.21.1-4)
+  void sdc(cd z, cd *sn, cd *cn, cd *dn) const {
+    const double m = 0.5;
+    const Jac a = jac(K * z.real(), m, K), b = jac(K * z.imag(), 1. - m, K);
+    const double den = b.cn * b.cn + m * a.sn * a.sn * b.sn * b.sn;
+    *sn = cd(a.sn * b.dn, a.cn * a.dn * b.sn * b.cn) / den;
+    *cn = cd(a.cn * b.cn, -a.sn * a.dn * b.sn * b.dn) / den;
+    *dn = cd(a.dn * b.cn * b.dn, -m * a.sn * a.cn * b.sn) / den;
+  }
+  // P(w) = (w - wc)(w + wc)(w^2 + wc^2)(w^4 + 7 + 4 sqrt 3), factored so that the
+  // zero at the corner keeps its relative accuracy
+  cd P(cd w) const {
+    const cd w2 = w * w;
+    return (w - wc) * (w + wc) * (w2 + wc * wc) * (w2 * w2 + (7. + 4. * std::sqrt(3.)));
+  }
+  cd dP(cd w) const {
+    const cd w3 = w * w * w;
+    return 8. * w3 * w3 * w + 56. * w3;
+  }
+  cd Dn(cd w) const {
+    const cd w4 = w * w * w * w, q = w4 - 1.;
+    return 108. * w4 * (q * q) * (q * q);
+  }
+  cd dDn(cd w) const {
+    const cd w3 = w * w * w, w4 = w3 * w, q = w4 - 1.;
+    return 432. * w3 * (q * q * q) * (5. * w4 - 1.);
+  }
+  // solve J_oct(w) = J_sq(z) near w0; returns false if Newton does not converge.
+  // Large |t| is solved in the form 1/J (the centre), small |t| as J (the corners).
+  bool solve(cd z, cd w0, cd *w_out, cd *fprime) const {
+    cd sn, cn, dn;
+    sdc(z, &sn, &cn, &dn);
+    const cd q = dn / sn;
+    const cd q2 = q * q;
+    const cd t = 4. * q2 * q2;  // J_sq
+    const bool inv = std::abs(t) > 1.;
+    const cd rt = inv ? 1. / t : t;
+    cd w = w0;
+    bool ok = false;
+    int polish = -1;  // once |dw| is below 1e-12 |w|, two more steps reach the rounding floor
+    for (int it = 0; it < 60; it++) {
+      const cd p = P(w), d = Dn(w);
+      cd F, dF;
+      if (inv) {
+        const cd p3 = p * p * p;
+        F = d / p3 - rt;
+        dF = (dDn(w) * p - 3. * d * dP(w)) / (p3 * p);
+      } else {
+        F = p * p * p / d - rt;
+        dF = (3. * p * p * dP(w) * d - p * p * p * dDn(w)) / (d * d);
+      }
+      const cd dw = F / dF;
+      w -= dw;
+      if (!std::isfinite(w.real()) || !std::isfinite(w.imag())) return false;
+      if (polish < 0 && std::abs(dw) <= 1e-12 * std::abs(w)) polish = 2;
+      if (polish >= 0 && polish-- == 0) {
+        ok = true;
+        break;
+      }
+    }
+    if (!ok) return false;
+    // f'(z) = dJ_sq/dz / dJ_oct/dw, in the same (J or 1/J) form
+    const cd p = P(w), d = Dn(w);
+    if (inv) {
+      const cd dsq = K * sn * sn * sn * cn / (dn * dn * dn * dn * dn);  // d(1/J_sq)/dz
+      const cd doc = (dDn(w) * p - 3. * d * dP(w)) / (p * p * p * p);   // d(1/J_oct)/dw
+      *fprime = dsq / doc;
+    } else {
+      const cd dsq = -16. * K * dn * dn * dn * cn / (sn * sn * sn * sn * sn);
+      const cd doc = (3. * p * p * dP(w) * d - p * p * p * dDn(w)) / (d * d);
+      *fprime = dsq / doc;
+    }
+    *w_out = w;
+    return true;
+  }
+  // w and f' at z in the fundamental triangle 0 <= Im z <= Re z <= 1 (z != 0)
+  bool fundamental(cd z, cd *w, cd *fp) const {
+    const cd vmid(1., 0.), vcor(1., 1.);
+    double tau = std::min(1., 0.05 / std::abs(z));
+    cd cur = tau * z;
+    cd wc_ = c1 * cur, fpc;
+    if (!solve(cur, wc_, &wc_, &fpc)) return false;
+    double h = 0.05;
+    int guard = 0;
+    while (tau < 1. && guard++ < 100000) {
+      const double dv = std::min(std::abs(tau * z - vmid), std::abs(tau * z - vcor));
+      const double hmax = std::max(1e-6, 0.25 * dv / std::abs(z));
+      double hh = std::min(std::min(h, hmax), 1. - tau);
+      const double tn = (1. - tau - hh < 1e-15) ? 1. : tau + hh;
+      const cd zn = tn * z;
+      const cd pred = wc_ + fpc * (zn - cur);
+      cd wn, fpn;
+      if (solve(zn, pred, &wn, &fpn) && std::abs(wn - pred) < 0.5 * std::abs(fpc * (zn - cur)) + 1e-14) {
+        tau = tn;
+        cur = zn;
+        wc_ = wn;
+        fpc = fpn;
+        h = std::min(0.1, 1.5 * hh);
+      } else {
+        h = 0.5 * hh;
+        if (h < 1e-9) return false;
+      }
+    }
+    *w = wc_;
+    *fp = fpc;
+    return true;
+  }
+};
+
+// Conformal map at face-local (X, Y): reduce to the fundamental triangle by the
+// face's 8 symmetries (the map commutes with them), then map back the point and
+// the real 2x2 Jacobian dw/d(X,Y).  `solve_fund` returns w and f' at a point of the
+// fundamental triangle (a cache of solved points, or a direct solve).
+template <class Fund>
+bool conformal_local(const Conformal &C, double X, double Y, double P[3], double dX[3], double dY[3],
+                     Fund &&solve_fund) {
+  const double sx = X < 0 ? -1. : 1., sy = Y < 0 ? -1. : 1.;
+  double a = std::fabs(X), b = std::fabs(Y);
+  const bool swap = b > a;
+  if (swap) std::swap(a, b);
+  double u, v, J[2][2];  // J[r][c] = d(u,v)_r / d(X,Y)_c
+  if (a == 0. && b == 0.) {
+    u = v = 0.;
+    J[0][0] = J[1][1] = C.c1;
+    J[0][1] = J[1][0] = 0.;
+  } else {
+    cd w, fp;
+    if (!solve_fund(a, b, &w, &fp)) return false;
+    u = w.real();
+    v = w.imag();
+    J[0][0] = fp.real(); J[0][1] = -fp.imag();
+    J[1][0] = fp.imag(); J[1][1] = fp.real();
+  }
+  if (swap) {  // reflection across the diagonal: M J M with M = [[0,1],[1,0]]
+    std::swap(u, v);
+    const double t00 = J[1][1], t01 = J[1][0], t10 = J[0][1], t11 = J[0][0];
+    J[0][0] = t00; J[0][1] = t01; J[1][0] = t10; J[1][1] = t11;
+  }
+  // sign flips: M = diag(sx, sy)
+  u *= sx;
+  v *= sy;
+  J[0][1] *= sx * sy;
+  J[1][0] *= sx * sy;
+  // inverse stereographic projection and its derivatives
+  const double r2 = u * u + v * v, D = 1. + r2, D2 = D * D;
+  P[0] = 2. * u / D;
+  P[1] = 2. * v / D;
+  P[2] = (1. - r2) / D;
+  const double xu = 2. * (1. + v * v - u * u) / D2, xv = -4. * u * v / D2;
+  const double yu = -4. * u * v / D2, yv = 2. * (1. + u * u - v * v) / D2;
+  const double zu = -4. * u / D2, zv = -4. * v / D2;
+  dX[0] = xu * J[0][0] + xv * J[1][0];
+  dX[1] = yu * J[0][0] + yv * J[1][0];
+  dX[2] = zu * J[0][0] + zv * J[1][0];
+  dY[0] = xu * J[0][1] + xv * J[1][1];
+  dY[1] = yu * J[0][1] + yv * J[1][1];
+  dY[2] = zu * J[0][1] + zv * J[1][1];
+  return true;
+}
+
+// global = R_p local with the panel frames of cuco.f90:89-105 (rotp0)
+void rotate_panel(int p, const double *v, double *g) {
+  switch (p) {
+    case 1: g[0] = v[2]; g[1] = v[0]; g[2] = v[1]; break;
+    case 2: g[0] = -v[0]; g[1] = v[2]; g[2] = v[1]; break;
+    case 3: g[0] = -v[2]; g[1] = -v[0]; g[2] = v[1]; break;
+    case 4: g[0] = v[0]; g[1] = -v[2]; g[2] = v[1]; break;
+    case 5: g[0] = -v[1]; g[1] = v[0]; g[2] = v[2]; break;
+    default: g[0] = v[1]; g[1] = v[0]; g[2] = -v[2]; break;
+  }
+}
+
+}  // namespace
+
+// Mesh-file samples at the cell centres: map coordinate of cell i is
+// xm = ((2i - 1) dx / 2 - 45) * 2/90 with dx = 90/N degrees
+// (mesh_generation/src/mesh_mod.f90:44-51); jab = dxc/dxm / 45 / D2R (:164).
 extern "C" int ccs_mesh_generate(int N, int map, double *lon_deg, double *lat_deg, double *x, double *y,
                                  double *z, double *jab) {
-  if (N < 1 || map != CCS_MAP_GNOMONIC_EQUIANGULAR || !lon_deg || !lat_deg || !x || !y || !z || !jab)
+  if (N < 1 || (map != CCS_MAP_GNOMONIC_EQUIANGULAR && map != CCS_MAP_CONFORMAL) || !lon_deg || !lat_deg || !x ||
+      !y || !z || !jab)
     return CCS_ERR_ARG;
   const double dx_deg = 90. / N;
+  const double scale = 1. / (45. * kD2R);
+  std::vector<double> lp((size_t)N * N * 9);
+  Conformal C;
+  // cell i and N+1-i sit at opposite X: cache the fundamental-triangle solutions by
+  // the pair (max, min) of distances-from-centre indices
+  const int half = (N + 1) / 2;
+  std::vector<cd> cw((size_t)half * half), cf((size_t)half * half);
+  std::vector<char> have((size_t)half * half, 0);
+  auto dist_index = [N](int i) { return (std::abs(2 * i - N - 1) - (N % 2 == 0 ? 1 : 0)) / 2; };
+  for (int j = 1; j <= N; j++)
+    for (int i = 1; i <= N; i++) {
+      const double X = ((2 * i - 1) * dx_deg / 2. - 45.) * (2. / 90.);
+      const double Y = ((2 * j - 1) * dx_deg / 2. - 45.) * (2. / 90.);
+      double *q = &lp[9 * ((size_t)(i - 1) + (size_t)N * (j - 1))];
+      if (map == CCS_MAP_GNOMONIC_EQUIANGULAR) {
+        gnomonic_local(X, Y, q, q + 3, q + 6);
+        continue;
+      }
+      int ia = dist_index(i), ib = dist_index(j);
+      if (ia < ib) std::swap(ia, ib);
+      const size_t key = (size_t)ia * half + ib;
+      auto fund = [&](double a, double b, cd *w, cd *fp) {
+        if (!have[key]) {
+          if (!C.fundamental(cd(a, b), &cw[key], &cf[key])) return false;
+          have[key] = 1;
+        }
+        *w = cw[key];
+        *fp = cf[key];
+        return true;
+      };
+      if (!conformal_local(C, X, Y, q, q + 3, q + 6, fund)) return CCS_ERR_MESH;
+    }
   for (int p = 1; p <= 6; p++)
     for (int j = 1; j <= N; j++)
       for (int i = 1; i <= N; i++) {
         const size_t s = (size_t)(i - 1) + (size_t)N * ((size_t)(j - 1) + (size_t)N * (size_t)(p - 1));
-        const double al = ((2 * i - 1) * dx_deg / 2. - 45.) * kD2R;
-        const double be = ((2 * j - 1) * dx_deg / 2. - 45.) * kD2R;
-        const double t = std::tan(al), u = std::tan(be);
-        const double rho = std::sqrt(1. + t * t + u * u);
-        const double r3 = rho * rho * rho;
-        const double l[3] = {t / rho, u / rho, 1. / rho};
-        const double da[3] = {(1. + t * t) * (1. + u * u) / r3, -(1. + t * t) * t * u / r3, -(1. + t * t) * t / r3};
-        const double db[3] = {-(1. + u * u) * t * u / r3, (1. + u * u) * (1. + t * t) / r3, -(1. + u * u) * u / r3};
-        // global = R_p local with the rotp0 columns of each panel
-        auto rot = [p](const double *v, double *g) {
-          switch (p) {
-            case 1: g[0] = v[2]; g[1] = v[0]; g[2] = v[1]; break;
-            case 2: g[0] = -v[0]; g[1] = v[2]; g[2] = v[1]; break;
-            case 3: g[0] = -v[2]; g[1] = -v[0]; g[2] = v[1]; break;
-            case 4: g[0] = v[0]; g[1] = -v[2]; g[2] = v[1]; break;
-            case 5: g[0] = -v[1]; g[1] = v[0]; g[2] = v[2]; break;
-            default: g[0] = v[1]; g[1] = v[0]; g[2] = -v[2]; break;
-          }
-        };
+        const double *q = &lp[9 * ((size_t)(i - 1) + (size_t)N * (j - 1))];
         double g[3], ga[3], gb[3];
-        rot(l, g);
-        rot(da, ga);
-        rot(db, gb);
+        rotate_panel(p, q, g);
+        rotate_panel(p, q + 3, ga);
+        rotate_panel(p, q + 6, gb);
         x[s] = g[0];
         y[s] = g[1];
         z[s] = g[2];
@@ -310,8 +588,8 @@ extern "C" int ccs_mesh_generate(int N, int map, double *lon_deg, double *lat_de
         lon_deg[s] = std::atan2(g[1], g[0]) * kR2D;
         lat_deg[s] = std::atan2(g[2], std::sqrt(g[0] * g[0] + g[1] * g[1])) * kR2D;
         for (int r = 0; r < 3; r++) {
-          jab[6 * s + r] = ga[r];
-          jab[6 * s + 3 + r] = gb[r];
+          jab[6 * s + r] = ga[r] * scale;
+          jab[6 * s + 3 + r] = gb[r] * scale;
         }
       }
   return CCS_OK;

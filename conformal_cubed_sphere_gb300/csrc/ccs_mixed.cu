@@ -186,7 +186,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         const float dP = fmaf(phibar, S.s[r + 1] - S.s[r], S.q[r + 1] - S.q[r]);
         const float uB = 0.5f * (S.uC[r] + S.uC[r + 1]);
         const float pB = 0.5f * (S.phit[r] + S.phit[r + 1]);
-        const float lam = fabsf(uB) + sqrtf(fmaxf(0.5f * (S.ig11[r] + S.ig11[r + 1]) * pB, 0.f));
+        const float lam = fabsf(uB) + sqrtf(fmaxf(0.5f * (S.ig11[r] + S.ig11[r + 1]) * pB * st.inv_a2, 0.f));
         S.gx[0][t] = 0.5f * (dF + S.Dx[0][cl] + S.Dx[1][cr] - lam * (dP + S.Dx[5][cr] - S.Dx[4][cl]));
         S.gx[1][t] = 0.5f * (dE + S.Dx[2][cl] + S.Dx[3][cr]);
       } else {
@@ -199,7 +199,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         const float dP = fmaf(phibar, S.s[r + RX] - S.s[r], S.q[r + RX] - S.q[r]);
         const float vB = 0.5f * (S.vC[r] + S.vC[r + RX]);
         const float pB = 0.5f * (S.phit[r] + S.phit[r + RX]);
-        const float lam = fabsf(vB) + sqrtf(fmaxf(0.5f * (S.ig22[r] + S.ig22[r + RX]) * pB, 0.f));
+        const float lam = fabsf(vB) + sqrtf(fmaxf(0.5f * (S.ig22[r] + S.ig22[r + RX]) * pB * st.inv_a2, 0.f));
         S.gy[0][yf] = 0.5f * (dG + S.Dy[0][cl] + S.Dy[1][cr] - lam * (dP + S.Dy[5][cr] - S.Dy[4][cl]));
         S.gy[1][yf] = 0.5f * (dE + S.Dy[2][cl] + S.Dy[3][cr]);
       }

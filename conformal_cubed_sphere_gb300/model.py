@@ -38,8 +38,9 @@ class Mesh:
     """Metric arrays of an N x N x 6 cubed sphere with `halo` ghost cells."""
 
     def __init__(self, N: int, halo: int = 3, radius: float = RADIUS, omega: float = OMEGA,
-                 gravity: float = GRAVITY, phis: np.ndarray | None = None):
+                 gravity: float = GRAVITY, phis: np.ndarray | None = None, cube_map: str = "conformal"):
         self.N, self.halo = int(N), int(halo)
+        self.cube_map = cube_map
         self.radius, self.omega, self.gravity = float(radius), float(omega), float(gravity)
         self.nh = self.N + 2 * self.halo
         self.ncell = self.nh * self.nh * 6
@@ -48,7 +49,8 @@ class Mesh:
         self.file = {k: np.zeros(n) for k in ("lon", "lat", "x", "y", "z")}
         self.file["jab"] = np.zeros(6 * n)
         f = self.file
-        L.check(lib.ccs_mesh_generate(self.N, L.CCS_MAP_GNOMONIC_EQUIANGULAR, _ptr(f["lon"]), _ptr(f["lat"]),
+        kind = {"conformal": L.CCS_MAP_CONFORMAL, "gnomonic": L.CCS_MAP_GNOMONIC_EQUIANGULAR}[cube_map]
+        L.check(lib.ccs_mesh_generate(self.N, kind, _ptr(f["lon"]), _ptr(f["lat"]),
                                       _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"])),
                 "ccs_mesh_generate")
         nc = self.ncell

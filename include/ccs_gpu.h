@@ -62,8 +62,10 @@ enum {
  * RECONSTRUCT fills them with WENO reconstructions of u at x-faces and v at y-faces. */
 enum { CCS_EDISS_ZERO = 0, CCS_EDISS_RECONSTRUCT = 1 };
 
-/* cube-to-sphere map used by the host mesh generator */
-enum { CCS_MAP_GNOMONIC_EQUIANGULAR = 0 };
+/* cube-to-sphere map used by the host mesh generator: the conformal cubic map of
+ * the reference mesh generator (gen_method 'Rancic', mesh_generation/src/
+ * mesh_mod.f90:150-171) or the equiangular gnomonic map */
+enum { CCS_MAP_GNOMONIC_EQUIANGULAR = 0, CCS_MAP_CONFORMAL = 1 };
 
 typedef struct ccs_config {
   int N;             /* cells along a panel edge: its = 1, ite = N (io_mod.F90:49-52) */

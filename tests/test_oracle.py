@@ -91,14 +91,22 @@ def test_halo_cells_are_geometric_neighbours():
     z = O.fill_halo(N, h, _cart(mesh, 2))
     F = mesh.field
     X, Y, Z = F(x), F(y), F(z)
-    ang = np.pi / 2 / N
+
+    def gap(i1, i2, p):
+        a = np.stack([X[i1, h:h + N, p], Y[i1, h:h + N, p], Z[i1, h:h + N, p]])
+        b = np.stack([X[i2, h:h + N, p], Y[i2, h:h + N, p], Z[i2, h:h + N, p]])
+        return np.arccos(np.clip(np.sum(a * b, axis=0), -1, 1))
+
+    away = slice(3, N - 3)  # rows away from the corner singularities
     for p in range(6):
+        # on the conformal grid the halo cells continue the panel's grid lines: the
+        # spacing across the edge matches the spacing just inside it
+        inside = gap(h, h + 1, p)
         for k in range(h):
-            # distance between consecutive cells across the left and right edges
-            a = np.stack([X[h - k, h:h + N, p], Y[h - k, h:h + N, p], Z[h - k, h:h + N, p]])
-            b = np.stack([X[h - k - 1, h:h + N, p], Y[h - k - 1, h:h + N, p], Z[h - k - 1, h:h + N, p]])
-            d = np.arccos(np.clip(np.sum(a * b, axis=0), -1, 1))
-            assert np.all(d < 1.6 * ang) and np.all(d > 0.5 * ang)
+            across = gap(h - k, h - k - 1, p)
+            r = across / inside
+            assert np.all(np.abs(r[away] - 1) < 0.2 + 0.15 * k), (p, k)
+            assert np.all((r > 0.2) & (r < 5))
 
 
 def _cart(mesh, comp):
