@@ -580,13 +580,13 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
   const double a2 = h->cfg.radius * h->cfg.radius;
   const size_t nf = (size_t)L.field, np = (size_t)L.panel;
   const size_t nref = (size_t)nh * nh * 6;
-  // shared: s ig11 ig12 ig21 ig22 inv_s (one panel each); per panel: phis fs
-  const size_t nfloat = 6 * np + 2 * nf;
+  // shared: s ig11 ig12 ig21 ig22 inv_s lamx lamy (one panel each); per panel: phis fs
+  const size_t nfloat = 8 * np + 2 * nf;
   CCS_TRY(h, cudaMalloc(&dm->buf32, nfloat * sizeof(float)));
   std::vector<float> hb(nfloat, 0.f);
-  float *sh[6];
-  for (int k = 0; k < 6; k++) sh[k] = hb.data() + k * np;
-  float *phs = hb.data() + 6 * np, *fs = phs + nf;
+  float *sh[8];
+  for (int k = 0; k < 8; k++) sh[k] = hb.data() + k * np;
+  float *phs = hb.data() + 8 * np, *fs = phs + nf;
   for (int p = 0; p < 6; p++)
     for (int j = 1 - hh; j <= N + hh; j++)
       for (int i = 1 - hh; i <= N + hh; i++) {
@@ -605,6 +605,15 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
         phs[d] = (float)mv->phis[r];
         fs[d] = (float)(mv->f[r] * sg / a2);
       }
+  // face wave-speed metric (spatial_operators_mod.F90:113-114, 138-139), x-faces i in
+  // [0, N] of rows j in [1, N] and y-faces j in [0, N] of columns i in [1, N]
+  for (int j = 0; j <= N; j++)
+    for (int i = 0; i <= N; i++) {
+      const size_t r = (size_t)(i + hh - 1) + (size_t)nh * (size_t)(j + hh - 1);
+      const int64_t d = L.idx(i, j, 0);
+      if (j >= 1) sh[6][d] = (float)(0.5 * (mv->matrixIG[4 * (r + 1)] + mv->matrixIG[4 * r]));
+      if (i >= 1) sh[7][d] = (float)(0.5 * (mv->matrixIG[4 * (r + nh) + 3] + mv->matrixIG[4 * r + 3]));
+    }
   CCS_TRY(h, cudaMemcpyAsync(dm->buf32, hb.data(), nfloat * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   // FP64 halo transforms, one per push-table entry: T = (G IA)_halo (A IG)_source
   const size_t ne = (size_t)24 * hh * N;
@@ -654,8 +663,10 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
   dm->mm.ig21 = dm->buf32 + 3 * np;
   dm->mm.ig22 = dm->buf32 + 4 * np;
   dm->mm.inv_s = dm->buf32 + 5 * np;
-  dm->mm.phis = dm->buf32 + 6 * np;
-  dm->mm.fs = dm->buf32 + 6 * np + nf;
+  dm->mm.lamx = dm->buf32 + 6 * np;
+  dm->mm.lamy = dm->buf32 + 7 * np;
+  dm->mm.phis = dm->buf32 + 8 * np;
+  dm->mm.fs = dm->buf32 + 8 * np + nf;
   dm->mm.xf = dxf;
   dm->mm.push = dm->push;
   (void)nref;

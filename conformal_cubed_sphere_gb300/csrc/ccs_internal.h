@@ -77,6 +77,9 @@ struct StateF64 {
 // the receiving halo cell's covariant wind (P2SP, fill, SP2P of correct_bdy_ghost).
 struct MeshMixed {
   const float *s, *ig11, *ig12, *ig21, *ig22, *inv_s;
+  // static wave-speed metric of the faces: lamx at the x-face right of cell (i, j)
+  // is (IG11(i,j) + IG11(i+1,j)) / 2, lamy likewise for the y-face above it
+  const float *lamx, *lamy;
   const float *phis, *fs;
   const double *xf;
   const int32_t *push;

@@ -83,7 +83,7 @@ cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp,
 
 // tile shapes
 constexpr int F64_TX = 32, F64_TY = 8, F64_THREADS = 256;
-constexpr int MX_TX = 32, MX_TY = 16, MX_THREADS = 256;
+constexpr int MX_TX = 32, MX_TY = 32, MX_THREADS = 256;
 
 // FP64 reductions (mass / energy) over the interior of an FP64 state
 cudaError_t launch_f64_diag(const Layout &L, const double *phiG, const double *phi, const double *u,

@@ -22,9 +22,11 @@ namespace ccs {
 namespace {
 
 constexpr int TX = MX_TX, TY = MX_TY, NT = MX_THREADS;
-constexpr int RX = TX + 6, RY = TY + 6, RN = RX * RY;
-constexpr int NCX = TY * (TX + 2), NCY = TX * (TY + 2), NC2 = NCX + NCY;
-constexpr int NFX = TY * (TX + 1), NFY = (TY + 1) * TX;
+constexpr int RX = TX + 6, RY = TY + 6;  // halo'd tile
+constexpr int SP = RX + 1;               // odd pitch: a warp reading one column hits 32 banks
+constexpr int RN = RY * SP;
+constexpr int NFL = TX + 1;              // faces per tile line
+static_assert(TX == 32 && TY == 32 && NT == 256, "lanes map to the 32 rows / columns of a tile");
 
 // Difference-form WENO-Z (spatial_operators_mod.F90:282-361) of one cell for both
 // directions.  d0..d3 = Q(c-1)-Q(c-2), Q(c)-Q(c-1), Q(c+1)-Q(c), Q(c+2)-Q(c+1).
@@ -53,8 +55,8 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
   const float m3 = fmaf(-2.f / 3.f, d1, (1.f / 6.f) * d0);
   // "+" weights
   {
-    const float a1 = 0.1f + 0.1f * r1, a2 = 0.6f + 0.6f * r2, a3 = 0.3f + 0.3f * r3;
-    float num = fmaf(a1, p1, fmaf(a2, p2, a3 * p3));
+    const float a1 = fmaf(0.1f, r1, 0.1f), a2 = fmaf(0.6f, r2, 0.6f), a3 = fmaf(0.3f, r3, 0.3f);
+    const float num = fmaf(a1, p1, fmaf(a2, p2, a3 * p3));
     float val = __fdividef(num, a1 + a2 + a3);
     if (t40 <= mn && t41 > mn) val = fmaf(1.f / 3.f, p1, (2.f / 3.f) * p2);
     else if (t40 > mn && t41 < mn) val = fmaf(2.f / 3.f, p2, (1.f / 3.f) * p3);
@@ -62,8 +64,8 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
   }
   // "-" weights: beta' = (b3, b2, b1), tau40' = t41, tau41' = t40
   {
-    const float a1 = 0.1f + 0.1f * r3, a2 = 0.6f + 0.6f * r2, a3 = 0.3f + 0.3f * r1;
-    float num = fmaf(a1, m1, fmaf(a2, m2, a3 * m3));
+    const float a1 = fmaf(0.1f, r3, 0.1f), a2 = fmaf(0.6f, r2, 0.6f), a3 = fmaf(0.3f, r1, 0.3f);
+    const float num = fmaf(a1, m1, fmaf(a2, m2, a3 * m3));
     float val = __fdividef(num, a1 + a2 + a3);
     if (t41 <= mn && t40 > mn) val = fmaf(1.f / 3.f, m1, (2.f / 3.f) * m2);
     else if (t41 > mn && t40 < mn) val = fmaf(2.f / 3.f, m2, (1.f / 3.f) * m3);
@@ -72,159 +74,166 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
 }
 
 struct SmemMx {
-  float uC[RN], vC[RN], F[RN], G[RN], E[RN], q[RN], s[RN], phit[RN], ig11[RN], ig22[RN], u[RN], v[RN];
-  float Dx[6][NCX];  // (DFp, DFm, DEp, DEm, DPp, DPm) at x-cells
-  float Dy[6][NCY];
-  float gx[2][NFX];  // (flux, E) face values relative to the left cell
-  float gy[2][NFY];
+  MixedStage st;  // this work item's stage descriptor
+  // cell quantities on the halo'd tile, [row][col] with pitch SP
+  float F[RN], G[RN], E[RN], hs[RN], s[RN], uC[RN], vC[RN], u[RN], v[RN];
+  float gx[2][TY][NFL];  // x-face (flux, E) values minus the value of the cell left of the face
+  float gy[2][NFL][TX];  // y-face values minus the value of the cell below the face
 };
 
 __device__ __forceinline__ bool corner(int i, int j, int N) { return (i < 1 || i > N) && (j < 1 || j > N); }
 
-__global__ void __launch_bounds__(NT, 2)
+// One tile line (a row for x-faces, a column for y-faces) from face f0 to f1:
+// the cells' difference windows slide along the line so that each cell costs one
+// new shared-memory value per field; the face between two cells is formed from
+// the left cell's "+" and the right cell's "-" corrections in registers.
+template <bool XDIR>
+__device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Qflux, const float *__restrict__ cvel,
+                                          const float *__restrict__ lam, const Layout &L, int lane, int f0, int f1,
+                                          int startg, int lineg) {
+  const MixedStage &st = S.st;
+  const float phibar = st.phibar, epsF = st.eps_F, epsE = st.eps_E, epsP = st.eps_P;
+  const int stp = XDIR ? 1 : SP;
+  const int base = XDIR ? (lane + 3) * SP + 2 : 2 * SP + lane + 3;  // cell ci = 0 of the line
+  int o = base + (f0 - 2) * stp;
+  // window values at cells c-2 .. c+1 for c = f0
+  float Fv[4], Ev[4], hv[4], sv[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    Fv[k] = Qflux[o + k * stp];
+    Ev[k] = S.E[o + k * stp];
+    hv[k] = S.hs[o + k * stp];
+    sv[k] = S.s[o + k * stp];
+  }
+  float dF0 = Fv[1] - Fv[0], dF1 = Fv[2] - Fv[1], dF2 = Fv[3] - Fv[2];
+  float dE0 = Ev[1] - Ev[0], dE1 = Ev[2] - Ev[1], dE2 = Ev[3] - Ev[2];
+  float q0 = hv[0] * sv[0], q1 = hv[1] * sv[1], q2 = hv[2] * sv[2], q3 = hv[3] * sv[3];
+  float dP0 = fmaf(phibar, sv[1] - sv[0], q1 - q0);
+  float dP1 = fmaf(phibar, sv[2] - sv[1], q2 - q1);
+  float dP2 = fmaf(phibar, sv[3] - sv[2], q3 - q2);
+  float Flast = Fv[3], Elast = Ev[3], slast = sv[3], qlast = q3;
+  float hc = hv[2], hc1 = hv[3];  // hs at c and c+1
+  float pDFp = 0.f, pDEp = 0.f, pDPp = 0.f, pU = 0.f, pH = 0.f;
+  for (int ci = f0; ci <= f1 + 1; ci++) {
+    const int on = base + (ci + 2) * stp;  // cell c+2
+    const float Fn = Qflux[on], En = S.E[on], hn = S.hs[on], sn = S.s[on];
+    const float qn = hn * sn;
+    const float dF3 = Fn - Flast, dE3 = En - Elast, dP3 = fmaf(phibar, sn - slast, qn - qlast);
+    float DFp, DFm, DEp, DEm, DPp, DPm;
+    weno_d(dF0, dF1, dF2, dF3, epsF, DFp, DFm);
+    weno_d(dE0, dE1, dE2, dE3, epsE, DEp, DEm);
+    weno_d(dP0, dP1, dP2, dP3, epsP, DPp, DPm);
+    const float uc = cvel[base + ci * stp];
+    if (ci > f0) {
+      const int fi = ci - 1;         // face between line cells ci-1 and ci
+      const int fg = startg + fi;    // global index of the cell left of / below the face
+      if (fg <= L.N) {
+        const int64_t cs = XDIR ? L.idx(fg, lineg, 0) : L.idx(lineg, fg, 0);
+        const float uB = 0.5f * (pU + uc);
+        const float pB = phibar + 0.5f * (pH + hc);
+        const float lm = fabsf(uB) + sqrtf(fmaxf(__ldg(lam + cs) * pB, 0.f));
+        const float gF = 0.5f * (dF1 + pDFp + DFm - lm * (dP1 + DPm - pDPp));
+        const float gE = 0.5f * (dE1 + pDEp + DEm);
+        if (XDIR) {
+          S.gx[0][lane][fi] = gF;
+          S.gx[1][lane][fi] = gE;
+        } else {
+          S.gy[0][fi][lane] = gF;
+          S.gy[1][fi][lane] = gE;
+        }
+      }
+    }
+    pDFp = DFp; pDEp = DEp; pDPp = DPp; pU = uc; pH = hc;
+    dF0 = dF1; dF1 = dF2; dF2 = dF3;
+    dE0 = dE1; dE1 = dE2; dE2 = dE3;
+    dP0 = dP1; dP1 = dP2; dP2 = dP3;
+    Flast = Fn; Elast = En; slast = sn; qlast = qn;
+    hc = hc1; hc1 = hn;
+  }
+}
+
+__global__ void __launch_bounds__(NT, 3)
 mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
   extern __shared__ __align__(16) float smem_f[];
   SmemMx &S = *reinterpret_cast<SmemMx *>(smem_f);
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const WorkItem wi = work[w];
-    const MixedStage &st = stages[wi.inst];
+    {  // stage descriptor into shared memory
+      const int nw = (int)(sizeof(MixedStage) / 4);
+      const int *src = reinterpret_cast<const int *>(stages + wi.inst);
+      int *dst = reinterpret_cast<int *>(&S.st);
+      for (int k = tid; k < nw; k += NT) dst[k] = src[k];
+    }
+    __syncthreads();
+    const MixedStage &st = S.st;
     const Layout L = st.L;
     const int N = L.N, p = wi.panel;
     const int i0 = 1 + wi.tx * TX, j0 = 1 + wi.ty * TY;
-    const float phibar = st.phibar;
-    const float a2 = st.a2;
 
-    // ---- phase 1: cell quantities -----------------------------------------
-    for (int r = tid; r < RN; r += NT) {
-      const int li = r % RX, lj = r / RX;
-      const int i = i0 - 3 + li, j = j0 - 3 + lj;
-      float uC = 0.f, vC = 0.f, F = 0.f, G = 0.f, E = 0.f, q = 0.f, s = 1.f, pt = 0.f, g11 = 0.f, g22 = 0.f,
-            u = 0.f, v = 0.f;
-      if (i >= -2 && i <= N + 3 && j >= -2 && j <= N + 3 && !corner(i, j, N)) {
-        const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
-        const float hp = st.in.hp[c];
-        u = st.in.u[c];
-        v = st.in.v[c];
-        const float phs = st.m.phis[c];
-        s = st.m.s[cs];
-        g11 = st.m.ig11[cs];
-        g22 = st.m.ig22[cs];
-        const float g12 = st.m.ig12[cs], g21 = st.m.ig21[cs];
-        uC = fmaf(g11, u, g12 * v);
-        vC = fmaf(g21, u, g22 * v);
-        const float mass = (phibar + hp) * s;  // phiG / a^2
-        F = mass * uC;
-        G = mass * vC;
-        const float hs = phs + hp;
-        E = fmaf(0.5f * a2, fmaf(u, uC, v * vC), hs);  // E - phibar
-        q = hs * s;                                     // phitG / a^2 - phibar s
-        pt = phibar + hs;
-      }
-      S.uC[r] = uC; S.vC[r] = vC; S.F[r] = F; S.G[r] = G; S.E[r] = E; S.q[r] = q; S.s[r] = s;
-      S.phit[r] = pt; S.ig11[r] = g11; S.ig22[r] = g22; S.u[r] = u; S.v[r] = v;
-    }
-    __syncthreads();
-
-    // ---- phase 2: difference-form WENO at cells ------------------------------
-    for (int t = tid; t < 3 * NC2; t += NT) {
-      const int fld = t / NC2, rem = t % NC2;
-      int r, stp, ok;
-      if (rem < NCX) {
-        const int ci = rem % (TX + 2), lj = rem / (TX + 2);
-        const int i = i0 - 1 + ci, j = j0 + lj;
-        ok = (i <= N + 1) && (j <= N);
-        r = (lj + 3) * RX + ci + 2;
-        stp = 1;
-      } else {
-        const int rr = rem - NCX;
-        const int li = rr % TX, cj = rr / TX;
-        const int i = i0 + li, j = j0 - 1 + cj;
-        ok = (i <= N) && (j <= N + 1);
-        r = (cj + 2) * RX + li + 3;
-        stp = RX;
-      }
-      float Dp = 0.f, Dm = 0.f;
-      if (ok) {
-        float d0, d1, d2, d3, eps;
-        if (fld == 2) {  // phitG: d = phibar ds + dq
-          const float *sq = S.q, *ss = S.s;
-          d0 = fmaf(phibar, ss[r - stp] - ss[r - 2 * stp], sq[r - stp] - sq[r - 2 * stp]);
-          d1 = fmaf(phibar, ss[r] - ss[r - stp], sq[r] - sq[r - stp]);
-          d2 = fmaf(phibar, ss[r + stp] - ss[r], sq[r + stp] - sq[r]);
-          d3 = fmaf(phibar, ss[r + 2 * stp] - ss[r + stp], sq[r + 2 * stp] - sq[r + stp]);
-          eps = st.eps_P;
-        } else {
-          const float *Q = (fld == 1) ? S.E : (stp == 1 ? S.F : S.G);
-          d0 = Q[r - stp] - Q[r - 2 * stp];
-          d1 = Q[r] - Q[r - stp];
-          d2 = Q[r + stp] - Q[r];
-          d3 = Q[r + 2 * stp] - Q[r + stp];
-          eps = (fld == 1) ? st.eps_E : st.eps_F;
+    // ---- phase 1: cell quantities on the halo'd tile ------------------------
+    {
+      const float phibar = st.phibar, ha2 = 0.5f * st.a2;
+      const float *__restrict__ ihp = st.in.hp, *__restrict__ iu = st.in.u, *__restrict__ iv = st.in.v;
+      const MeshMixed m = st.m;
+      for (int r = tid; r < RX * RY; r += NT) {
+        const int li = r % RX, lj = r / RX;
+        const int i = i0 - 3 + li, j = j0 - 3 + lj;
+        float F = 0.f, G = 0.f, E = 0.f, hs = 0.f, sc = 1.f, uC = 0.f, vC = 0.f, u = 0.f, v = 0.f;
+        if (i <= N + 3 && j <= N + 3 && !corner(i, j, N)) {
+          const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
+          const float hp = __ldg(ihp + c);
+          u = __ldg(iu + c);
+          v = __ldg(iv + c);
+          sc = __ldg(m.s + cs);
+          uC = fmaf(__ldg(m.ig11 + cs), u, __ldg(m.ig12 + cs) * v);
+          vC = fmaf(__ldg(m.ig21 + cs), u, __ldg(m.ig22 + cs) * v);
+          const float mass = (phibar + hp) * sc;  // phiG / a^2
+          F = mass * uC;
+          G = mass * vC;
+          hs = __ldg(m.phis + c) + hp;
+          E = fmaf(ha2, fmaf(u, uC, v * vC), hs);  // E - phibar
         }
-        weno_d(d0, d1, d2, d3, eps, Dp, Dm);
-      }
-      if (rem < NCX) {
-        S.Dx[2 * fld][rem] = Dp;
-        S.Dx[2 * fld + 1][rem] = Dm;
-      } else {
-        S.Dy[2 * fld][rem - NCX] = Dp;
-        S.Dy[2 * fld + 1][rem - NCX] = Dm;
+        const int a = lj * SP + li;
+        S.F[a] = F; S.G[a] = G; S.E[a] = E; S.hs[a] = hs; S.s[a] = sc;
+        S.uC[a] = uC; S.vC[a] = vC; S.u[a] = u; S.v[a] = v;
       }
     }
     __syncthreads();
 
-    // ---- phase 3: Rusanov face values relative to the left / lower cell --------
-    for (int t = tid; t < NFX + NFY; t += NT) {
-      if (t < NFX) {
-        const int fi = t % (TX + 1), lj = t / (TX + 1);
-        const int r = (lj + 3) * RX + fi + 2;  // cell f; f+1 at r+1
-        const int cl = lj * (TX + 2) + fi, cr = cl + 1;
-        const float dF = S.F[r + 1] - S.F[r];
-        const float dE = S.E[r + 1] - S.E[r];
-        const float dP = fmaf(phibar, S.s[r + 1] - S.s[r], S.q[r + 1] - S.q[r]);
-        const float uB = 0.5f * (S.uC[r] + S.uC[r + 1]);
-        const float pB = 0.5f * (S.phit[r] + S.phit[r + 1]);
-        const float lam = fabsf(uB) + sqrtf(fmaxf(0.5f * (S.ig11[r] + S.ig11[r + 1]) * pB * st.inv_a2, 0.f));
-        S.gx[0][t] = 0.5f * (dF + S.Dx[0][cl] + S.Dx[1][cr] - lam * (dP + S.Dx[5][cr] - S.Dx[4][cl]));
-        S.gx[1][t] = 0.5f * (dE + S.Dx[2][cl] + S.Dx[3][cr]);
+    // ---- phase 2: lines -> face values (warps 0-3 rows, 4-7 columns) ---------
+    {
+      const int seg = warp & 3;
+      const int f0 = seg == 0 ? 0 : 1 + 8 * seg;  // faces 0-8, 9-16, 17-24, 25-32
+      const int f1 = 8 + 8 * seg;
+      if (warp < 4) {
+        if (j0 + lane <= N) tile_line<true>(S, S.F, S.uC, st.m.lamx, L, lane, f0, f1, i0 - 1, j0 + lane);
       } else {
-        const int yf = t - NFX;
-        const int li = yf % TX, fj = yf / TX;
-        const int r = (fj + 2) * RX + li + 3;  // cell g; g+1 at r+RX
-        const int cl = fj * TX + li, cr = cl + TX;
-        const float dG = S.G[r + RX] - S.G[r];
-        const float dE = S.E[r + RX] - S.E[r];
-        const float dP = fmaf(phibar, S.s[r + RX] - S.s[r], S.q[r + RX] - S.q[r]);
-        const float vB = 0.5f * (S.vC[r] + S.vC[r + RX]);
-        const float pB = 0.5f * (S.phit[r] + S.phit[r + RX]);
-        const float lam = fabsf(vB) + sqrtf(fmaxf(0.5f * (S.ig22[r] + S.ig22[r + RX]) * pB * st.inv_a2, 0.f));
-        S.gy[0][yf] = 0.5f * (dG + S.Dy[0][cl] + S.Dy[1][cr] - lam * (dP + S.Dy[5][cr] - S.Dy[4][cl]));
-        S.gy[1][yf] = 0.5f * (dE + S.Dy[2][cl] + S.Dy[3][cr]);
+        if (i0 + lane <= N) tile_line<false>(S, S.G, S.vC, st.m.lamy, L, lane, f0, f1, j0 - 1, i0 + lane);
       }
     }
     __syncthreads();
 
-    // ---- phase 4: tendencies, stage update, ghost push -------------------------
-    for (int t = tid; t < TX * TY; t += NT) {
-      const int li = t % TX, lj = t / TX;
+    // ---- phase 3: tendencies, stage update, ghost push -------------------------
+#pragma unroll 1
+    for (int k = 0; k < 4; k++) {
+      const int li = lane, lj = warp + 8 * k;
       const int i = i0 + li, j = j0 + lj;
       if (i > N || j > N) continue;
-      const int r = (lj + 3) * RX + li + 3;
-      const int xl = lj * (TX + 1) + li, yb = lj * TX + li;
-      const float divx = (S.gx[0][xl + 1] - S.gx[0][xl] + (S.F[r] - S.F[r - 1])) * st.rdx;
-      const float dEdx = (S.gx[1][xl + 1] - S.gx[1][xl] + (S.E[r] - S.E[r - 1])) * st.rdx;
-      const float divy = (S.gy[0][yb + TX] - S.gy[0][yb] + (S.G[r] - S.G[r - RX])) * st.rdy;
-      const float dEdy = (S.gy[1][yb + TX] - S.gy[1][yb] + (S.E[r] - S.E[r - RX])) * st.rdy;
+      const int r = (lj + 3) * SP + li + 3;
+      const float divx = (S.gx[0][lj][li + 1] - S.gx[0][lj][li] + (S.F[r] - S.F[r - 1])) * st.rdx;
+      const float dEdx = (S.gx[1][lj][li + 1] - S.gx[1][lj][li] + (S.E[r] - S.E[r - 1])) * st.rdx;
+      const float divy = (S.gy[0][lj + 1][li] - S.gy[0][lj][li] + (S.G[r] - S.G[r - SP])) * st.rdy;
+      const float dEdy = (S.gy[1][lj + 1][li] - S.gy[1][lj][li] + (S.E[r] - S.E[r - SP])) * st.rdy;
       const float *vv = S.v + r, *uu = S.u + r;
       const float dvdx = (-vv[-3] + 9.f * vv[-2] - 45.f * vv[-1] + 45.f * vv[1] - 9.f * vv[2] + vv[3]) * st.rdx60;
-      const float dudy = (-uu[-3 * RX] + 9.f * uu[-2 * RX] - 45.f * uu[-RX] + 45.f * uu[RX] - 9.f * uu[2 * RX] +
-                          uu[3 * RX]) *
+      const float dudy = (-uu[-3 * SP] + 9.f * uu[-2 * SP] - 45.f * uu[-SP] + 45.f * uu[SP] - 9.f * uu[2 * SP] +
+                          uu[3 * SP]) *
                          st.rdy60;
       const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
-      const float vort = dvdx - dudy + st.m.fs[c];
-      const float tp = -(divx + divy) * st.m.inv_s[cs];
+      const float vort = dvdx - dudy + __ldg(st.m.fs + c);
+      const float tp = -(divx + divy) * __ldg(st.m.inv_s + cs);
       const float tu = fmaf(vort, S.vC[r], -dEdx * st.inv_a2);
       const float tv = fmaf(-vort, S.uC[r], -dEdy * st.inv_a2);
       if (st.kind == K_TEND) {
@@ -241,13 +250,12 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
           st.acchp[c] = tp; st.accu[c] = tu; st.accv[c] = tv;
           ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
           break;
-        case K_RK4_2: {
+        case K_RK4_2:
           st.acchp[c] = fmaf(2.f, tp, st.acchp[c]);
           st.accu[c] = fmaf(2.f, tu, st.accu[c]);
           st.accv[c] = fmaf(2.f, tv, st.accv[c]);
           ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
           break;
-        }
         case K_RK4_4: {
           const float k6 = st.c1 * (1.f / 6.f);
           ip = k6 * (st.acchp[c] + tp); iu = k6 * (st.accu[c] + tu); iv = k6 * (st.accv[c] + tv);
@@ -276,12 +284,13 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         const float hi[3] = {y0p, y0u, y0v};
         const float inc[3] = {ip, iu, iv};
         float out[3];
-        for (int k = 0; k < 3; k++) {
-          const float y = inc[k] + lo[k];
-          const float tt = hi[k] + y;
-          const float bp = tt - hi[k];
-          lo[k] = (hi[k] - (tt - bp)) + (y - bp);
-          out[k] = tt;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const float y = inc[q] + lo[q];
+          const float tt = hi[q] + y;
+          const float bp = tt - hi[q];
+          lo[q] = (hi[q] - (tt - bp)) + (y - bp);
+          out[q] = tt;
         }
         np = out[0]; nu = out[1]; nv = out[2];
         st.lohp[c] = lo[0]; st.lou[c] = lo[1]; st.lov[c] = lo[2];
@@ -294,21 +303,23 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       // ghost push: hp copies; the covariant wind crosses the edge through the
       // FP64 2x2 transform G_h IA_h A_s IG_s of the receiving halo cell
       const int h = L.h;
-      for (int side = 0; side < 4; side++) {
-        int k, m;
-        if (side == 0) { k = i; m = j; }
-        else if (side == 1) { k = N + 1 - i; m = j; }
-        else if (side == 2) { k = j; m = i; }
-        else { k = N + 1 - j; m = i; }
-        if (k > h) continue;
-        const int64_t e = ((int64_t)p * 4 + side) * h * N + (int64_t)(k - 1) * N + (m - 1);
-        const int64_t d = st.m.push[e];
-        const double *T = st.m.xf + 4 * e;
-        const double ud = T[0] * (double)nu + T[1] * (double)nv;
-        const double vd = T[2] * (double)nu + T[3] * (double)nv;
-        st.out.hp[d] = np;
-        st.out.u[d] = (float)ud;
-        st.out.v[d] = (float)vd;
+      if (i <= h || j <= h || i > N - h || j > N - h) {
+        for (int side = 0; side < 4; side++) {
+          int kk, m;
+          if (side == 0) { kk = i; m = j; }
+          else if (side == 1) { kk = N + 1 - i; m = j; }
+          else if (side == 2) { kk = j; m = i; }
+          else { kk = N + 1 - j; m = i; }
+          if (kk > h) continue;
+          const int64_t e = ((int64_t)p * 4 + side) * h * N + (int64_t)(kk - 1) * N + (m - 1);
+          const int64_t d = st.m.push[e];
+          const double *T = st.m.xf + 4 * e;
+          const double ud = T[0] * (double)nu + T[1] * (double)nv;
+          const double vd = T[2] * (double)nu + T[3] * (double)nv;
+          st.out.hp[d] = np;
+          st.out.u[d] = (float)ud;
+          st.out.v[d] = (float)vd;
+        }
       }
     }
     __syncthreads();
