@@ -85,6 +85,7 @@ SIGNATURES = {
     "ccs_ghost_map": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     "ccs_timing": (C.c_int, [_vp, C.c_int, C.c_int, _dp, C.POINTER(C.c_int64)]),
     "ccs_stream": (C.c_void_p, [_vp]),
+    "ccs_selftest_div": (C.c_int, [_dp, C.c_int64, C.c_double, _dp, _dp]),
     "ccs_strerror": (C.c_char_p, [C.c_int]),
     "ccs_last_error": (C.c_char_p, [_vp]),
     "ccs_abi_version": (C.c_int, []),

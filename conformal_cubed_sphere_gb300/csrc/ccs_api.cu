@@ -337,6 +337,28 @@ int ccs_abi_version(void) { return CCS_ABI_VERSION; }
 
 void *ccs_stream(ccs_handle *h) { return h ? (void *)h->stream : nullptr; }
 
+int ccs_selftest_div(const double *x, int64_t n, double b, double *fast, double *ieee) {
+  if (!x || n <= 0 || !fast || !ieee) return CCS_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CCS_ERR_NODEVICE;
+  cudaSetDevice(0);
+  double *dx = nullptr, *dout = nullptr;
+  if (cudaMalloc(&dx, n * sizeof(double)) != cudaSuccess) return CCS_ERR_NOMEM;
+  if (cudaMalloc(&dout, 2 * n * sizeof(double)) != cudaSuccess) {
+    cudaFree(dx);
+    return CCS_ERR_NOMEM;
+  }
+  int rc = CCS_OK;
+  if (cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      launch_div_const_check(dx, n, b, dout, 0) != cudaSuccess ||
+      cudaMemcpy(fast, dout, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(ieee, dout + n, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = CCS_ERR_CUDA;
+  cudaFree(dx);
+  cudaFree(dout);
+  return rc;
+}
+
 const char *ccs_strerror(int status) {
   switch (status) {
     case CCS_OK: return "ok";

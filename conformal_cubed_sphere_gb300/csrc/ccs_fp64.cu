@@ -29,16 +29,33 @@ constexpr int NFX = TY * (TX + 1), NFY = (TY + 1) * TX, NF = NFX + NFY;
 constexpr int NCELL_ARR = 11;
 static_assert(TX * TY == NT, "phase 3 maps one thread to one cell");
 
+}  // namespace
+
+// x / b for the constant divisors b = 3, 6, 12 of the reference (x/3., x/6.,
+// A*A*13./12.), correctly rounded: q0 = RN(x y) with y = RN(1/b), the remainder
+// r = x - q0 b is exact in one FMA, and q0 + r y rounded once is RN(x / b)
+// (Markstein's correction, IBM J. Res. Dev. 34(1), 1990).  A zero dividend keeps its
+// sign through q0.  The GPU test suite checks this against IEEE division.
+__device__ __forceinline__ double ccs_div_const(double x, double b, double y) {
+  const double q0 = x * y;
+  const double r = fma(-q0, b, x);
+  const double q1 = fma(r, y, q0);
+  return x == 0.0 ? q0 : q1;
+}
+
+namespace {
+
 // WENO_limiter, spatial_operators_mod.F90:282-361.
 template <int DIR>
 __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double q3, double q4) {
   // q0..q4 = Q(1..5) = field(i-2 .. i+2)
   const double Qim2 = q0, Qim1 = q1, Qi = q2, Qip1 = q3, Qip2 = q4;
   double s0, s1, s2, a0, a1, a2, b0, b1, b2;
+  const double y3 = 1. / 3., y6 = 1. / 6., y12 = 1. / 12.;
   if (DIR > 0) {
-    s0 = Qim2 / 3. - 7. / 6. * Qim1 + 11. / 6. * Qi;
-    s1 = -Qim1 / 6. + 5. / 6. * Qi + 1. / 3. * Qip1;
-    s2 = Qi / 3. + 5. / 6. * Qip1 - 1. / 6. * Qip2;
+    s0 = ccs_div_const(Qim2, 3., y3) - 7. / 6. * Qim1 + 11. / 6. * Qi;
+    s1 = ccs_div_const(-Qim1, 6., y6) + 5. / 6. * Qi + 1. / 3. * Qip1;
+    s2 = ccs_div_const(Qi, 3., y3) + 5. / 6. * Qip1 - 1. / 6. * Qip2;
     a0 = Qim2 - 2. * Qim1 + Qi;
     a1 = Qim1 - 2. * Qi + Qip1;
     a2 = Qi - 2. * Qip1 + Qip2;
@@ -46,9 +63,9 @@ __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double
     b1 = Qim1 - Qip1;
     b2 = 3. * Qi - 4. * Qip1 + Qip2;
   } else {
-    s0 = Qip2 / 3. - 7. / 6. * Qip1 + 11. / 6. * Qi;
-    s1 = -Qip1 / 6. + 5. / 6. * Qi + 1. / 3. * Qim1;
-    s2 = Qi / 3. + 5. / 6. * Qim1 - 1. / 6. * Qim2;
+    s0 = ccs_div_const(Qip2, 3., y3) - 7. / 6. * Qip1 + 11. / 6. * Qi;
+    s1 = ccs_div_const(-Qip1, 6., y6) + 5. / 6. * Qi + 1. / 3. * Qim1;
+    s2 = ccs_div_const(Qi, 3., y3) + 5. / 6. * Qim1 - 1. / 6. * Qim2;
     a0 = Qip2 - 2. * Qip1 + Qi;
     a1 = Qip1 - 2. * Qi + Qim1;
     a2 = Qi - 2. * Qim1 + Qim2;
@@ -56,9 +73,9 @@ __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double
     b1 = Qip1 - Qim1;
     b2 = 3. * Qi - 4. * Qim1 + Qim2;
   }
-  const double be0 = a0 * a0 * 13. / 12. + b0 * b0 * 0.25;
-  const double be1 = a1 * a1 * 13. / 12. + b1 * b1 * 0.25;
-  const double be2 = a2 * a2 * 13. / 12. + b2 * b2 * 0.25;
+  const double be0 = ccs_div_const(a0 * a0 * 13., 12., y12) + b0 * b0 * 0.25;
+  const double be1 = ccs_div_const(a1 * a1 * 13., 12., y12) + b1 * b1 * 0.25;
+  const double be2 = ccs_div_const(a2 * a2 * 13., 12., y12) + b2 * b2 * 0.25;
   const double tau40 = fabs(be0 - be1);
   const double tau41 = fabs(be1 - be2);
   const double tau5 = fabs(be2 - be0);
@@ -251,9 +268,9 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
               break;
             }
             case K_RK4_4: {
-              const double kp = (st.accphiG[c] + tp) / 6.;
-              const double ku = (st.accu[c] + tu) / 6.;
-              const double kv = (st.accv[c] + tv) / 6.;
+              const double kp = ccs_div_const(st.accphiG[c] + tp, 6., 1. / 6.);
+              const double ku = ccs_div_const(st.accu[c] + tu, 6., 1. / 6.);
+              const double kv = ccs_div_const(st.accv[c] + tv, 6., 1. / 6.);
               np = y0p + st.c1 * kp; nu = y0u + st.c1 * ku; nv = y0v + st.c1 * kv;
               break;
             }
@@ -322,6 +339,20 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
 }
 
 }  // namespace
+
+// test support: out[k] = ccs_div_const(x[k], b, 1/b) next to out[n + k] = x[k] / b
+__global__ void div_const_check_kernel(const double *__restrict__ x, int64_t n, double b, double y,
+                                       double *__restrict__ out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    out[k] = ccs_div_const(x[k], b, y);
+    out[n + k] = x[k] / b;
+  }
+}
+
+cudaError_t launch_div_const_check(const double *x, int64_t n, double b, double *out, cudaStream_t s) {
+  div_const_check_kernel<<<1024, 256, 0, s>>>(x, n, b, 1. / b, out);
+  return cudaGetLastError();
+}
 
 int f64_stage_smem_bytes(int ediss) {
   return (int)((NCELL_ARR * RN + (ediss ? 8 : 6) * NF) * sizeof(double));

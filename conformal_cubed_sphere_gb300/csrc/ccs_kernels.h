@@ -85,6 +85,9 @@ cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp,
 constexpr int F64_TX = 32, F64_TY = 8, F64_THREADS = 256;
 constexpr int MX_TX = 32, MX_TY = 32, MX_THREADS = 256;
 
+// test support: correctly rounded division by a constant, see ccs_fp64.cu
+cudaError_t launch_div_const_check(const double *x, int64_t n, double b, double *out, cudaStream_t s);
+
 // FP64 reductions (mass / energy) over the interior of an FP64 state
 cudaError_t launch_f64_diag(const Layout &L, const double *phiG, const double *phi, const double *u,
                             const double *v, const double *uC, const double *vC, const double *sqrtG,

@@ -170,6 +170,12 @@ int ccs_ghost_map(int N, int halo, int64_t *src_index);
  * with CUDA events on the handle's stream when timing is enabled. */
 int ccs_timing(ccs_handle *h, int enable, int reset, double *kernel_ms, int64_t *launches);
 
+/* Self-check of the FP64 lane's division by the constants 3, 6 and 12: for each
+ * x[k] the device computes the correctly rounded quotient the kernels use (fast[k])
+ * and the IEEE quotient x[k] / b (ieee[k]); they must agree bit for bit.  Runs on
+ * device 0 with temporary buffers. */
+int ccs_selftest_div(const double *x, int64_t n, double b, double *fast, double *ieee);
+
 /* The CUDA stream (a cudaStream_t) every launch of this handle is ordered on, so
  * that a caller can place its own events or copies before and after a step. */
 void *ccs_stream(ccs_handle *h);

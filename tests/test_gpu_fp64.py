@@ -145,3 +145,26 @@ def test_reference_test_cases_run():
         m = valid_mask(mesh)
         for k in CHECK_FIELDS:
             assert bitwise_equal(g[k], o[k], m), (kind, k)
+
+
+@pytest.mark.parametrize("b", [3.0, 6.0, 12.0])
+def test_constant_division_is_correctly_rounded(b):
+    """The FP64 lane divides by the constants 3, 6 and 12 with a reciprocal and one
+    FMA correction; every quotient must equal IEEE division bit for bit."""
+    import ctypes as C
+    rng = np.random.default_rng(int(b))
+    n = 1 << 23
+    sig = rng.integers(0, 1 << 52, size=n, dtype=np.uint64)
+    exp = rng.integers(1023 - 200, 1023 + 200, size=n, dtype=np.uint64)
+    sgn = rng.integers(0, 2, size=n, dtype=np.uint64)
+    x = ((sgn << np.uint64(63)) | (exp << np.uint64(52)) | sig).view(np.float64).copy()
+    # exact multiples, halfway-style significands and signed zeros
+    x[:8] = [0.0, -0.0, 3.0, -6.0, 1.0, 1.5, 2.0 ** -40, 7.0]
+    x[8:4096] = np.arange(8, 4096) * b
+    fast = np.empty(n)
+    ieee = np.empty(n)
+    dp = C.POINTER(C.c_double)
+    rc = L.lib().ccs_selftest_div(x.ctypes.data_as(dp), n, b, fast.ctypes.data_as(dp), ieee.ctypes.data_as(dp))
+    assert rc == 0
+    assert np.array_equal(fast.view(np.int64), ieee.view(np.int64))
+    assert np.array_equal(ieee, x / b)
