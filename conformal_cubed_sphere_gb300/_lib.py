@@ -19,6 +19,8 @@ CCS_ERR_UNSUPPORTED = 5
 CCS_ERR_MESH = 6
 CCS_ERR_NOMEM = 7
 CCS_ERR_NODEVICE = 8
+CCS_ERR_TOO_LARGE = 9
+CCS_NOALLOC_MAX_N = 4096
 
 CCS_RK4 = 0
 CCS_RK3_TVD = 1
@@ -79,6 +81,7 @@ SIGNATURES = {
     "ccs_sync": (C.c_int, [_vp]),
     "ccs_spatial_operator": (C.c_int, [_vp, _dp, _dp, _dp]),
     "ccs_diag": (C.c_int, [_vp, _dp, _dp]),
+    "ccs_diag_noalloc": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 9 + [_vp]),
     "ccs_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
     "ccs_batch_step": (C.c_int, [_vp, C.c_int]),
     "ccs_batch_destroy": (None, [_vp]),

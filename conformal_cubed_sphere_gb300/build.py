@@ -27,6 +27,7 @@ UNITS = [
     ("ccs_mixed.cu", []),
     ("ccs_api.cu", []),
     ("ccs_host.cpp", []),
+    ("ccs_noalloc.cu", []),
 ]
 
 

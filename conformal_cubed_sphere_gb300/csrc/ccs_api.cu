@@ -370,6 +370,7 @@ const char *ccs_strerror(int status) {
     case CCS_ERR_MESH: return "singular or inconsistent mesh";
     case CCS_ERR_NOMEM: return "out of memory";
     case CCS_ERR_NODEVICE: return "no CUDA device";
+    case CCS_ERR_TOO_LARGE: return "size exceeds the fixed scratch capacity";
     default: return "unknown status";
   }
 }

@@ -43,7 +43,8 @@ enum {
   CCS_ERR_UNSUPPORTED = 5, /* option not available in this build */
   CCS_ERR_MESH = 6,        /* singular metric (io_mod.F90:176-188 stops here) */
   CCS_ERR_NOMEM = 7,       /* device or host allocation failed */
-  CCS_ERR_NODEVICE = 8     /* no CUDA device visible */
+  CCS_ERR_NODEVICE = 8,    /* no CUDA device visible */
+  CCS_ERR_TOO_LARGE = 9    /* size above a fixed capacity (ccs_diag_noalloc) */
 };
 
 /* integral_scheme (parameters_mod.F90:402-408) */
@@ -149,6 +150,23 @@ int ccs_spatial_operator(ccs_handle *h, double *tend_phiG, double *tend_u, doubl
 /* calc_total_mass / calc_total_energy (diag_mod.F90:10-53) of the current state,
  * as FP64 sums on the device. */
 int ccs_diag(ccs_handle *h, double *total_mass, double *total_energy);
+
+/* Total mass and energy, like ccs_diag, of a state that already lives in device
+ * memory, without allocating anything.  This entry point has no counterpart in the
+ * reference.  It serves callers that cannot call cudaMalloc (code running inside
+ * another framework's memory pool or a fixed device arena, or being captured into
+ * a CUDA graph).  All array arguments are device pointers in the reference layout
+ * (ics:ice, jcs:jce, 6); mass_energy is a device pointer to two doubles; stream is a
+ * cudaStream_t (NULL for the legacy default stream) and the call returns once the
+ * work is enqueued.  Its scratch is a fixed device array sized for N up to
+ * CCS_NOALLOC_MAX_N (larger N returns CCS_ERR_TOO_LARGE); every GPU that loads the
+ * library holds that array until exit.  The first call on a device looks up the
+ * array's device address, so make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race, so order them on one stream. */
+#define CCS_NOALLOC_MAX_N 4096
+int ccs_diag_noalloc(int N, int halo, const double *phiG, const double *phi, const double *u,
+                     const double *v, const double *uC, const double *vC, const double *sqrtG,
+                     const double *phis, double *mass_energy, void *stream);
 
 /* ---- ensembles and uneven batches ---------------------------------------- */
 
