@@ -48,10 +48,8 @@ ALG_BYTES_FP64 = 600.0
 
 
 def _dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from conformal_cubed_sphere_gb300.parallel import dist_env
+    return dist_env()
 
 
 class ClockSampler:
@@ -264,10 +262,8 @@ def main():
     with sampler:
         t_mixed = time_device_steps(mixed, torch, args.steps, flush)
     barrier()
-    if ws > 1:
-        t = torch.tensor([t_mixed], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_mixed = float(t.item())
+    from conformal_cubed_sphere_gb300.parallel import slowest_rank_seconds
+    t_mixed = slowest_rank_seconds(t_mixed)
     value = ws * cells * args.steps / t_mixed
 
     # roofline of the dominant kernel (the mixed stage kernel)
