@@ -39,7 +39,9 @@ def _nvcc() -> str:
 
 
 def _common(nvcc: str) -> list[str]:
-    return [
+    # CCS_BUILD_FLAGS: extra nvcc flags (tuning macros such as -DCCS_MIXED_MIN_CTAS=3)
+    extra = os.environ.get("CCS_BUILD_FLAGS", "").split()
+    return extra + [
         nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
         "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", f"-I{CSRC}", f"-I{PKG.parent / 'include'}",
     ]

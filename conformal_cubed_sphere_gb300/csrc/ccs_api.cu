@@ -603,12 +603,12 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
   const double a2 = h->cfg.radius * h->cfg.radius;
   const size_t nf = (size_t)L.field, np = (size_t)L.panel;
   const size_t nref = (size_t)nh * nh * 6;
-  // shared: s ig11 ig12 ig21 ig22 inv_s lamx lamy (one panel each); per panel: phis fs
-  const size_t nfloat = 8 * np + 2 * nf;
+  // shared: s inv_s lamx lamy (one panel each) + ig as float4; per panel: phis fs
+  const size_t nfloat = 8 * np + 2 * nf;  // s, inv_s, lamx, lamy, ig (4 per cell), phis, fs
   CCS_TRY(h, cudaMalloc(&dm->buf32, nfloat * sizeof(float)));
   std::vector<float> hb(nfloat, 0.f);
-  float *sh[8];
-  for (int k = 0; k < 8; k++) sh[k] = hb.data() + k * np;
+  float *sh_s = hb.data(), *sh_inv = hb.data() + np, *sh_lamx = hb.data() + 2 * np, *sh_lamy = hb.data() + 3 * np;
+  float *sh_ig = hb.data() + 4 * np;  // interleaved (11, 12, 21, 22), 16-byte aligned (np % 4 == 0)
   float *phs = hb.data() + 8 * np, *fs = phs + nf;
   for (int p = 0; p < 6; p++)
     for (int j = 1 - hh; j <= N + hh; j++)
@@ -618,12 +618,12 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
         const double sg = mv->sqrtG[r];
         if (p == 0) {
           const double *IG = &mv->matrixIG[4 * r];
-          sh[0][d] = (float)(sg / a2);
-          sh[1][d] = (float)(IG[0] * a2);
-          sh[2][d] = (float)(IG[2] * a2);
-          sh[3][d] = (float)(IG[1] * a2);
-          sh[4][d] = (float)(IG[3] * a2);
-          sh[5][d] = sg > 0. ? (float)(a2 / sg) : 0.f;
+          sh_s[d] = (float)(sg / a2);
+          sh_ig[4 * d + 0] = (float)(IG[0] * a2);
+          sh_ig[4 * d + 1] = (float)(IG[2] * a2);
+          sh_ig[4 * d + 2] = (float)(IG[1] * a2);
+          sh_ig[4 * d + 3] = (float)(IG[3] * a2);
+          sh_inv[d] = sg > 0. ? (float)(a2 / sg) : 0.f;
         }
         phs[d] = (float)mv->phis[r];
         fs[d] = (float)(mv->f[r] * sg / a2);
@@ -634,8 +634,8 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
     for (int i = 0; i <= N; i++) {
       const size_t r = (size_t)(i + hh - 1) + (size_t)nh * (size_t)(j + hh - 1);
       const int64_t d = L.idx(i, j, 0);
-      if (j >= 1) sh[6][d] = (float)(0.5 * (mv->matrixIG[4 * (r + 1)] + mv->matrixIG[4 * r]));
-      if (i >= 1) sh[7][d] = (float)(0.5 * (mv->matrixIG[4 * (r + nh) + 3] + mv->matrixIG[4 * r + 3]));
+      if (j >= 1) sh_lamx[d] = (float)(0.5 * (mv->matrixIG[4 * (r + 1)] + mv->matrixIG[4 * r]));
+      if (i >= 1) sh_lamy[d] = (float)(0.5 * (mv->matrixIG[4 * (r + nh) + 3] + mv->matrixIG[4 * r + 3]));
     }
   CCS_TRY(h, cudaMemcpyAsync(dm->buf32, hb.data(), nfloat * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   // FP64 halo transforms, one per push-table entry: T = (G IA)_halo (A IG)_source
@@ -681,13 +681,10 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
   CCS_TRY(h, cudaStreamSynchronize(h->stream));
   dm->xf = dxf;
   dm->mm.s = dm->buf32;
-  dm->mm.ig11 = dm->buf32 + np;
-  dm->mm.ig12 = dm->buf32 + 2 * np;
-  dm->mm.ig21 = dm->buf32 + 3 * np;
-  dm->mm.ig22 = dm->buf32 + 4 * np;
-  dm->mm.inv_s = dm->buf32 + 5 * np;
-  dm->mm.lamx = dm->buf32 + 6 * np;
-  dm->mm.lamy = dm->buf32 + 7 * np;
+  dm->mm.inv_s = dm->buf32 + np;
+  dm->mm.lamx = dm->buf32 + 2 * np;
+  dm->mm.lamy = dm->buf32 + 3 * np;
+  dm->mm.ig = reinterpret_cast<const float4 *>(dm->buf32 + 4 * np);
   dm->mm.phis = dm->buf32 + 8 * np;
   dm->mm.fs = dm->buf32 + 8 * np + nf;
   dm->mm.xf = dxf;

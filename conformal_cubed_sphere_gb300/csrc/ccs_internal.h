@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <vector>
 
+#include <vector_types.h>
+
 #include "../../include/ccs_gpu.h"
 
 #if defined(__CUDACC__)
@@ -76,7 +78,9 @@ struct StateF64 {
 // the FP64 2x2 matrix G_h IA_h A_s IG_s taking the source cell's covariant wind to
 // the receiving halo cell's covariant wind (P2SP, fill, SP2P of correct_bdy_ghost).
 struct MeshMixed {
-  const float *s, *ig11, *ig12, *ig21, *ig22, *inv_s;
+  const float *s, *inv_s;
+  const float4 *ig;  // (IG11, IG12, IG21, IG22) * a^2 of each cell of the panel
+
   // static wave-speed metric of the faces: lamx at the x-face right of cell (i, j)
   // is (IG11(i,j) + IG11(i+1,j)) / 2, lamy likewise for the y-face above it
   const float *lamx, *lamy;

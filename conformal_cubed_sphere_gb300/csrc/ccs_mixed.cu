@@ -37,10 +37,11 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
                                        float &Dm) {
   const float A1 = d1 - d0, A2 = d2 - d1, A3 = d3 - d2;
   const float B1 = fmaf(3.f, d1, -d0), B2 = d1 + d2, B3 = fmaf(-3.f, d2, d3);
-  const float c1312 = 13.f / 12.f;
-  const float b1 = fmaf(c1312 * A1, A1, 0.25f * B1 * B1);
-  const float b2 = fmaf(c1312 * A2, A2, 0.25f * B2 * B2);
-  const float b3 = fmaf(c1312 * A3, A3, 0.25f * B3 * B3);
+  // 4 beta_k (eps is passed times 4 as well: the weights depend on ratios only)
+  const float k133 = 13.f / 3.f;
+  const float b1 = fmaf(k133 * A1, A1, B1 * B1);
+  const float b2 = fmaf(k133 * A2, A2, B2 * B2);
+  const float b3 = fmaf(k133 * A3, A3, B3 * B3);
   const float t40 = fabsf(b1 - b2), t41 = fabsf(b2 - b3), t5 = fabsf(b3 - b1);
   const float mn = fminf(b1, fminf(b2, b3));
   const float r1 = __fdividef(t5, eps + b1);
@@ -53,23 +54,25 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
   const float m1 = fmaf(-5.f / 6.f, d2, (1.f / 3.f) * d3);
   const float m2 = fmaf(-1.f / 6.f, d2, -(1.f / 3.f) * d1);
   const float m3 = fmaf(-2.f / 3.f, d1, (1.f / 6.f) * d0);
-  // "+" weights
-  {
+  // the two hard switches of the reference select fixed weights; computed
+  // unconditionally and selected, so no branch diverges
+  const float sa = fmaf(1.f / 3.f, p1, (2.f / 3.f) * p2), sb = fmaf(2.f / 3.f, p2, (1.f / 3.f) * p3);
+  const float ta = fmaf(1.f / 3.f, m1, (2.f / 3.f) * m2), tb = fmaf(2.f / 3.f, m2, (1.f / 3.f) * m3);
+  const bool lo40 = t40 <= mn, lo41 = t41 <= mn, hi40 = t40 > mn, hi41 = t41 > mn;
+  const bool lt40 = t40 < mn, lt41 = t41 < mn;
+  {  // "+" weights
     const float a1 = fmaf(0.1f, r1, 0.1f), a2 = fmaf(0.6f, r2, 0.6f), a3 = fmaf(0.3f, r3, 0.3f);
     const float num = fmaf(a1, p1, fmaf(a2, p2, a3 * p3));
     float val = __fdividef(num, a1 + a2 + a3);
-    if (t40 <= mn && t41 > mn) val = fmaf(1.f / 3.f, p1, (2.f / 3.f) * p2);
-    else if (t40 > mn && t41 < mn) val = fmaf(2.f / 3.f, p2, (1.f / 3.f) * p3);
-    Dp = val;
+    val = (hi40 && lt41) ? sb : val;
+    Dp = (lo40 && hi41) ? sa : val;
   }
-  // "-" weights: beta' = (b3, b2, b1), tau40' = t41, tau41' = t40
-  {
+  {  // "-" weights: beta' = (b3, b2, b1), tau40' = t41, tau41' = t40
     const float a1 = fmaf(0.1f, r3, 0.1f), a2 = fmaf(0.6f, r2, 0.6f), a3 = fmaf(0.3f, r1, 0.3f);
     const float num = fmaf(a1, m1, fmaf(a2, m2, a3 * m3));
     float val = __fdividef(num, a1 + a2 + a3);
-    if (t41 <= mn && t40 > mn) val = fmaf(1.f / 3.f, m1, (2.f / 3.f) * m2);
-    else if (t41 > mn && t40 < mn) val = fmaf(2.f / 3.f, m2, (1.f / 3.f) * m3);
-    Dm = val;
+    val = (hi41 && lt40) ? tb : val;
+    Dm = (lo41 && hi40) ? ta : val;
   }
 }
 
@@ -89,10 +92,10 @@ __device__ __forceinline__ bool corner(int i, int j, int N) { return (i < 1 || i
 // the left cell's "+" and the right cell's "-" corrections in registers.
 template <bool XDIR>
 __device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Qflux, const float *__restrict__ cvel,
-                                          const float *__restrict__ lam, const Layout &L, int lane, int f0, int f1,
-                                          int startg, int lineg) {
+                                          const float *__restrict__ lam, const Layout &L, int lane, int f0,
+                                          int NFACE, int startg, int lineg) {
   const MixedStage &st = S.st;
-  const float phibar = st.phibar, epsF = st.eps_F, epsE = st.eps_E, epsP = st.eps_P;
+  const float phibar = st.phibar, epsF = 4.f * st.eps_F, epsE = 4.f * st.eps_E, epsP = 4.f * st.eps_P;
   const int stp = XDIR ? 1 : SP;
   const int base = XDIR ? (lane + 3) * SP + 2 : 2 * SP + lane + 3;  // cell ci = 0 of the line
   int o = base + (f0 - 2) * stp;
@@ -114,7 +117,18 @@ __device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Q
   float Flast = Fv[3], Elast = Ev[3], slast = sv[3], qlast = q3;
   float hc = hv[2], hc1 = hv[3];  // hs at c and c+1
   float pDFp = 0.f, pDEp = 0.f, pDPp = 0.f, pU = 0.f, pH = 0.f;
-  for (int ci = f0; ci <= f1 + 1; ci++) {
+  // face wave-speed metric, fetched one face ahead of its use (the index is clamped
+  // into the panel so the prefetch never leaves the array)
+  auto lam_at = [&](int fi) -> float {
+    int fg = startg + fi;
+    fg = fg < 0 ? 0 : (fg > L.N ? L.N : fg);
+    return __ldg(lam + (XDIR ? L.idx(fg, lineg, 0) : L.idx(lineg, fg, 0)));
+  };
+  float lam_next = lam_at(f0);
+  for (int k = 0; k <= NFACE; k++) {
+    const int ci = f0 + k;
+    const float lam_cur = lam_next;
+    if (k > 0 && k < NFACE) lam_next = lam_at(ci);
     const int on = base + (ci + 2) * stp;  // cell c+2
     const float Fn = Qflux[on], En = S.E[on], hn = S.hs[on], sn = S.s[on];
     const float qn = hn * sn;
@@ -124,14 +138,13 @@ __device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Q
     weno_d(dE0, dE1, dE2, dE3, epsE, DEp, DEm);
     weno_d(dP0, dP1, dP2, dP3, epsP, DPp, DPm);
     const float uc = cvel[base + ci * stp];
-    if (ci > f0) {
+    if (k > 0) {
       const int fi = ci - 1;         // face between line cells ci-1 and ci
       const int fg = startg + fi;    // global index of the cell left of / below the face
       if (fg <= L.N) {
-        const int64_t cs = XDIR ? L.idx(fg, lineg, 0) : L.idx(lineg, fg, 0);
         const float uB = 0.5f * (pU + uc);
         const float pB = phibar + 0.5f * (pH + hc);
-        const float lm = fabsf(uB) + sqrtf(fmaxf(__ldg(lam + cs) * pB, 0.f));
+        const float lm = fabsf(uB) + sqrtf(fmaxf(lam_cur * pB, 0.f));
         const float gF = 0.5f * (dF1 + pDFp + DFm - lm * (dP1 + DPm - pDPp));
         const float gE = 0.5f * (dE1 + pDEp + DEm);
         if (XDIR) {
@@ -152,7 +165,12 @@ __device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Q
   }
 }
 
-__global__ void __launch_bounds__(NT, 3)
+// resident CTAs per SM the register allocation targets (3: 80 registers)
+#ifndef CCS_MIXED_MIN_CTAS
+#define CCS_MIXED_MIN_CTAS 3
+#endif
+
+__global__ void __launch_bounds__(NT, CCS_MIXED_MIN_CTAS)
 mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
   extern __shared__ __align__(16) float smem_f[];
   SmemMx &S = *reinterpret_cast<SmemMx *>(smem_f);
@@ -177,6 +195,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       const float phibar = st.phibar, ha2 = 0.5f * st.a2;
       const float *__restrict__ ihp = st.in.hp, *__restrict__ iu = st.in.u, *__restrict__ iv = st.in.v;
       const MeshMixed m = st.m;
+#pragma unroll 2
       for (int r = tid; r < RX * RY; r += NT) {
         const int li = r % RX, lj = r / RX;
         const int i = i0 - 3 + li, j = j0 - 3 + lj;
@@ -187,8 +206,9 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
           u = __ldg(iu + c);
           v = __ldg(iv + c);
           sc = __ldg(m.s + cs);
-          uC = fmaf(__ldg(m.ig11 + cs), u, __ldg(m.ig12 + cs) * v);
-          vC = fmaf(__ldg(m.ig21 + cs), u, __ldg(m.ig22 + cs) * v);
+          const float4 g = __ldg(m.ig + cs);
+          uC = fmaf(g.x, u, g.y * v);
+          vC = fmaf(g.z, u, g.w * v);
           const float mass = (phibar + hp) * sc;  // phiG / a^2
           F = mass * uC;
           G = mass * vC;
@@ -206,17 +226,17 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     {
       const int seg = warp & 3;
       const int f0 = seg == 0 ? 0 : 1 + 8 * seg;  // faces 0-8, 9-16, 17-24, 25-32
-      const int f1 = 8 + 8 * seg;
+      const int nface = seg == 0 ? 9 : 8;
       if (warp < 4) {
-        if (j0 + lane <= N) tile_line<true>(S, S.F, S.uC, st.m.lamx, L, lane, f0, f1, i0 - 1, j0 + lane);
+        if (j0 + lane <= N) tile_line<true>(S, S.F, S.uC, st.m.lamx, L, lane, f0, nface, i0 - 1, j0 + lane);
       } else {
-        if (i0 + lane <= N) tile_line<false>(S, S.G, S.vC, st.m.lamy, L, lane, f0, f1, j0 - 1, i0 + lane);
+        if (i0 + lane <= N) tile_line<false>(S, S.G, S.vC, st.m.lamy, L, lane, f0, nface, j0 - 1, i0 + lane);
       }
     }
     __syncthreads();
 
     // ---- phase 3: tendencies, stage update, ghost push -------------------------
-#pragma unroll 1
+#pragma unroll
     for (int k = 0; k < 4; k++) {
       const int li = lane, lj = warp + 8 * k;
       const int i = i0 + li, j = j0 + lj;
@@ -300,26 +320,47 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       st.out.hp[c] = np;
       st.out.u[c] = nu;
       st.out.v[c] = nv;
-      // ghost push: hp copies; the covariant wind crosses the edge through the
-      // FP64 2x2 transform G_h IA_h A_s IG_s of the receiving halo cell
+    }
+    __syncthreads();
+
+    // ---- phase 4: ghost push of the tile's edge strips ----------------------
+    // hp copies; the covariant wind crosses the edge through the FP64 2x2
+    // transform G_h IA_h A_s IG_s of the receiving halo cell.  Entries are dealt
+    // out to threads in push-table order, so no lane idles behind an edge lane.
+    if (st.kind != K_TEND) {
       const int h = L.h;
-      if (i <= h || j <= h || i > N - h || j > N - h) {
-        for (int side = 0; side < 4; side++) {
-          int kk, m;
-          if (side == 0) { kk = i; m = j; }
-          else if (side == 1) { kk = N + 1 - i; m = j; }
-          else if (side == 2) { kk = j; m = i; }
-          else { kk = N + 1 - j; m = i; }
-          if (kk > h) continue;
-          const int64_t e = ((int64_t)p * 4 + side) * h * N + (int64_t)(kk - 1) * N + (m - 1);
-          const int64_t d = st.m.push[e];
-          const double *T = st.m.xf + 4 * e;
-          const double ud = T[0] * (double)nu + T[1] * (double)nv;
-          const double vd = T[2] * (double)nu + T[3] * (double)nv;
-          st.out.hp[d] = np;
-          st.out.u[d] = (float)ud;
-          st.out.v[d] = (float)vd;
-        }
+      // strips: 0 left (k = i), 1 right (k = N+1-i), 2 below (k = j), 3 above (k = N+1-j);
+      // each tile pushes the strip cells it owns: cross-edge range [xlo, xhi]
+      // (i for left/right, j for below/above) and along-edge range [alo, ahi]
+      const int ie = min(i0 + TX - 1, N), je = min(j0 + TY - 1, N);
+      int xlo[4], xhi[4], alo[4], ahi[4], off[5];
+      xlo[0] = i0; xhi[0] = min(ie, h); alo[0] = j0; ahi[0] = je;
+      xlo[1] = max(i0, N - h + 1); xhi[1] = ie; alo[1] = j0; ahi[1] = je;
+      xlo[2] = j0; xhi[2] = min(je, h); alo[2] = i0; ahi[2] = ie;
+      xlo[3] = max(j0, N - h + 1); xhi[3] = je; alo[3] = i0; ahi[3] = ie;
+      off[0] = 0;
+      for (int sd = 0; sd < 4; sd++) {
+        const int nx = xhi[sd] - xlo[sd] + 1, na = ahi[sd] - alo[sd] + 1;
+        off[sd + 1] = off[sd] + (nx > 0 && na > 0 ? nx * na : 0);
+      }
+      for (int t = tid; t < off[4]; t += NT) {
+        int sd = 0;
+        while (t >= off[sd + 1]) sd++;
+        const int q = t - off[sd];
+        const int na = ahi[sd] - alo[sd] + 1;
+        const int x = xlo[sd] + q / na, m = alo[sd] + q % na;
+        const int k = (sd == 0 || sd == 2) ? x : N + 1 - x;
+        const int i = sd < 2 ? x : m, j = sd < 2 ? m : x;
+        const int64_t c = L.idx(i, j, p);
+        const int64_t e = ((int64_t)p * 4 + sd) * h * N + (int64_t)(k - 1) * N + (m - 1);
+        const int64_t d = st.m.push[e];
+        const double *T = st.m.xf + 4 * e;
+        const float np = st.out.hp[c], nu = st.out.u[c], nv = st.out.v[c];
+        const double ud = T[0] * (double)nu + T[1] * (double)nv;
+        const double vd = T[2] * (double)nu + T[3] * (double)nv;
+        st.out.hp[d] = np;
+        st.out.u[d] = (float)ud;
+        st.out.v[d] = (float)vd;
       }
     }
     __syncthreads();
