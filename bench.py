@@ -222,8 +222,100 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _batch_time(batch, torch, steps: int):
+    st = torch.cuda.ExternalStream(batch.stream_ptr)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(st)
+    batch.step_async(steps)
+    ev1.record(st)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3
+
+
+def run_ensemble(args, torch):
+    """64 members at C96 (seed + k, RMS 150-250 m, wind 30-50 m/s), mixed lane, one
+    launch per RK stage for all members, graph-captured; against the same members
+    advanced one after another through their own handles."""
+    from conformal_cubed_sphere_gb300 import model as M
+    n, N = args.members, 96
+    mesh = M.Mesh(N, HALO)
+    states = [M.ensemble_member_state(mesh, k, seed=SEED) for k in range(n)]
+    dts = [M.cfl_dt(mesh, st, 0.5) for st in states]
+    phibar = 8000.0 * mesh.gravity
+    owner = M.Stepper(mesh, dts[0], precision="mixed", phi_mean=phibar)
+    members = [owner] + [M.Stepper(mesh, dts[k], precision="mixed", phi_mean=phibar, share_with=owner)
+                         for k in range(1, n)]
+    for st, m in zip(states, members):
+        m.set_state(st)
+    batch = M.Batch(members)
+    batch.step(max(args.warmup, 3))
+    t_batch = _batch_time(batch, torch, args.steps)
+    # sequential: the same members, one handle after another
+    for m in members:
+        m.step(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for m in members:
+        m.step(args.steps)
+    t_seq = time.perf_counter() - t0
+    cells = 6 * N * N * n
+    rate = n * args.steps / t_batch
+    print(json.dumps({
+        "metric": "ensemble member-steps/s (64 x C96, mixed lane)", "value": rate, "unit": "member-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_batch / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 metric transforms)",
+        "data": "synthetic (seeded spherical harmonics)",
+        "config": {"workload": f"{n} members at C{N}, seed+k, RMS U[150,250] m, wind U[30,50] m/s, RK4, CFL 0.5",
+                   "l2": "inputs larger than L2 (all members' state)"},
+        "cell_steps_per_s": cells * args.steps / t_batch,
+        "sequential": {"value": n * args.steps / t_seq, "unit": "member-steps/s",
+                       "how": "each member's own handle (graph per step), one after another, host-timed"},
+        "batch_over_sequential": t_seq / t_batch,
+        "hbm": {"alg_GBs": ALG_BYTES_MIXED * cells * args.steps / t_batch / 1e9, "peak": _peaks()[0]},
+    }))
+
+
+def run_uneven(args, torch):
+    """16 x C48 + 8 x C96 + 4 x C192 + 1 x C384, per-instance CFL dt; one member of
+    each resolution below C384 on the FP64 lane, the others mixed."""
+    from conformal_cubed_sphere_gb300 import model as M
+    groups = [(48, 16), (96, 8), (192, 4), (384, 1)]
+    members, cells64, cells32, k = [], 0, 0, 0
+    for N, cnt in groups:
+        mesh = M.Mesh(N, HALO)
+        for c in range(cnt):
+            lane = "fp64" if (c == 0 and N < 384) else "mixed"
+            st = M.ensemble_member_state(mesh, k, seed=SEED, lmax_oro=8)
+            dt = M.cfl_dt(mesh, st, 0.5)
+            m = M.Stepper(mesh, dt, precision=lane, phi_mean=8000.0 * mesh.gravity)
+            m.set_state(st)
+            members.append(m)
+            if lane == "fp64":
+                cells64 += 6 * N * N
+            else:
+                cells32 += 6 * N * N
+            k += 1
+    batch = M.Batch(members)
+    batch.step(max(args.warmup, 3))
+    t = _batch_time(batch, torch, args.steps)
+    cells = cells64 + cells32
+    alg = (ALG_BYTES_FP64 * cells64 + ALG_BYTES_MIXED * cells32) * args.steps / t / 1e9
+    print(json.dumps({
+        "metric": "uneven batch cell-steps/s (16xC48 + 8xC96 + 4xC192 + 1xC384)", "value": cells * args.steps / t,
+        "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 mixed + f64", "data": "synthetic (seeded spherical harmonics)",
+        "config": {"workload": "29 instances, per-instance CFL dt, one FP64 member per resolution below C384",
+                   "fp64_cells": cells64, "mixed_cells": cells32, "l2": "inputs larger than L2"},
+        "hbm": {"alg_GBs": alg, "peak": _peaks()[0], "frac": alg / _peaks()[0]},
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="c384", choices=["c384", "ensemble", "uneven"])
+    ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=5)
@@ -238,6 +330,12 @@ def main():
     ws, rank, local = _dist()
     import torch
     torch.cuda.set_device(local)
+    if args.workload == "ensemble":
+        run_ensemble(args, torch)
+        return
+    if args.workload == "uneven":
+        run_uneven(args, torch)
+        return
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))

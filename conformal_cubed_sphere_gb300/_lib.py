@@ -84,6 +84,8 @@ SIGNATURES = {
     "ccs_diag_noalloc": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 9 + [_vp]),
     "ccs_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
     "ccs_batch_step": (C.c_int, [_vp, C.c_int]),
+    "ccs_batch_step_async": (C.c_int, [_vp, C.c_int]),
+    "ccs_batch_stream": (C.c_void_p, [_vp]),
     "ccs_batch_destroy": (None, [_vp]),
     "ccs_ghost_map": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     "ccs_timing": (C.c_int, [_vp, C.c_int, C.c_int, _dp, C.POINTER(C.c_int64)]),

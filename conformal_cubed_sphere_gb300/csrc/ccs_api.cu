@@ -934,36 +934,45 @@ struct BatchGroup {
   void *d_stages = nullptr;  // [n_rk + 1][nmem] F64Stage or MixedStage (last row: F64 final with sphere winds)
   WorkItem *d_work = nullptr;
   int nwork = 0, grid = 0;
+  cudaStream_t stream = nullptr;  // groups are independent: each runs on its own stream
+  cudaEvent_t done = nullptr;
 };
 
 struct ccs_batch {
   std::vector<BatchGroup> groups;
   std::vector<ccs_handle *> members;
   cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
   int device = 0;
   cudaGraphExec_t g_step = nullptr, g_step_sw = nullptr;
   std::string err;
 };
 
+// One step of every group: the groups fork from the batch stream, run their RK
+// stages on their own streams (an FP64 group is FP64-issue bound and a mixed group
+// FP32 / latency bound, so they share the SMs well) and join back.
 static int batch_enqueue(ccs_batch *b, bool with_sw) {
-  const int maxrk = 4;
-  for (int k = 0; k < maxrk; k++)
-    for (auto &g : b->groups) {
-      if (k >= g.n_rk) continue;
+  if (cudaEventRecord(b->fork, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  for (auto &g : b->groups) {
+    if (cudaStreamWaitEvent(g.stream, b->fork, 0) != cudaSuccess) return CCS_ERR_CUDA;
+    for (int k = 0; k < g.n_rk; k++) {
       cudaError_t e;
       if (g.lane == CCS_FP64) {
         const int row = (k == g.n_rk - 1 && with_sw) ? g.n_rk : k;
         e = launch_f64_stage((const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork, g.grid,
-                             b->stream);
+                             g.stream);
       } else {
         e = launch_mixed_stage((const MixedStage *)g.d_stages + (size_t)k * g.nmem, g.d_work, g.nwork, g.grid,
-                               b->stream);
+                               g.stream);
       }
       if (e != cudaSuccess) {
         b->err = cudaGetErrorString(e);
         return CCS_ERR_CUDA;
       }
     }
+    if (cudaEventRecord(g.done, g.stream) != cudaSuccess) return CCS_ERR_CUDA;
+    if (cudaStreamWaitEvent(b->stream, g.done, 0) != cudaSuccess) return CCS_ERR_CUDA;
+  }
   return CCS_OK;
 }
 
@@ -981,6 +990,7 @@ extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **o
   b->device = dev;
   b->members.assign(members, members + n);
   cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   for (int lane = 0; lane < 2; lane++)
     for (int scheme = 0; scheme < 2; scheme++) {
       BatchGroup g;
@@ -990,6 +1000,8 @@ extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **o
       if (g.members.empty()) continue;
       g.nmem = (int)g.members.size();
       g.n_rk = scheme == CCS_RK4 ? 4 : 3;
+      cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+      cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
       std::vector<WorkItem> work;
       const int TXg = lane == CCS_FP64 ? F64_TX : MX_TX, TYg = lane == CCS_FP64 ? F64_TY : MX_TY;
       for (int m = 0; m < g.nmem; m++) {
@@ -1040,12 +1052,10 @@ static int batch_capture(ccs_batch *b, bool with_sw, cudaGraphExec_t *out) {
   return e == cudaSuccess ? CCS_OK : CCS_ERR_CUDA;
 }
 
-extern "C" int ccs_batch_step(ccs_batch *b, int nsteps) {
+static int batch_step(ccs_batch *b, int nsteps, bool sync) {
   if (!b || nsteps < 0) return CCS_ERR_ARG;
   if (nsteps == 0) return CCS_OK;
   cudaSetDevice(b->device);
-  // members' own streams may hold pending work (set_state is synchronous, so
-  // nothing is pending here); the batch runs on its own stream
   if (!b->g_step) {
     int rc = batch_capture(b, false, &b->g_step);
     if (!rc) rc = batch_capture(b, true, &b->g_step_sw);
@@ -1054,10 +1064,14 @@ extern "C" int ccs_batch_step(ccs_batch *b, int nsteps) {
   for (int s = 0; s < nsteps - 1; s++)
     if (cudaGraphLaunch(b->g_step, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
   if (cudaGraphLaunch(b->g_step_sw, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
-  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  if (sync && cudaStreamSynchronize(b->stream) != cudaSuccess) return CCS_ERR_CUDA;
   for (ccs_handle *h : b->members) h->sphere_valid = true;
   return CCS_OK;
 }
+
+extern "C" int ccs_batch_step(ccs_batch *b, int nsteps) { return batch_step(b, nsteps, true); }
+extern "C" int ccs_batch_step_async(ccs_batch *b, int nsteps) { return batch_step(b, nsteps, false); }
+extern "C" void *ccs_batch_stream(ccs_batch *b) { return b ? (void *)b->stream : nullptr; }
 
 extern "C" void ccs_batch_destroy(ccs_batch *b) {
   if (!b) return;
@@ -1068,7 +1082,10 @@ extern "C" void ccs_batch_destroy(ccs_batch *b) {
   for (auto &g : b->groups) {
     if (g.d_stages) cudaFree(g.d_stages);
     if (g.d_work) cudaFree(g.d_work);
+    if (g.done) cudaEventDestroy(g.done);
+    if (g.stream) cudaStreamDestroy(g.stream);
   }
+  if (b->fork) cudaEventDestroy(b->fork);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }

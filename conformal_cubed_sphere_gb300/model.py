@@ -155,6 +155,16 @@ def ghost_map(N: int, halo: int) -> np.ndarray:
     return out
 
 
+def ensemble_member_state(mesh: Mesh, k: int, seed: int = 1, lmax_oro: int = 0) -> State:
+    """Member k of a seeded ensemble: seed + k, perturbation RMS drawn uniformly in
+    150-250 m and maximum wind in 30-50 m/s from the member's own generator."""
+    rng = np.random.default_rng(seed + k)
+    h_rms = float(rng.uniform(150.0, 250.0))
+    wind = float(rng.uniform(30.0, 50.0))
+    return initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=seed + k, h_rms=h_rms, wind_max=wind,
+                         lmax_oro=lmax_oro)
+
+
 class Stepper:
     """One instance of the GPU step (a ccs_handle)."""
 
@@ -242,6 +252,13 @@ class Batch:
 
     def step(self, nsteps: int = 1):
         L.check(L.lib().ccs_batch_step(self.handle, int(nsteps)), "ccs_batch_step")
+
+    def step_async(self, nsteps: int = 1):
+        L.check(L.lib().ccs_batch_step_async(self.handle, int(nsteps)), "ccs_batch_step_async")
+
+    @property
+    def stream_ptr(self) -> int:
+        return L.lib().ccs_batch_stream(self.handle) or 0
 
     def close(self):
         if self.handle:

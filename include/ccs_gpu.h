@@ -174,6 +174,9 @@ int ccs_diag_noalloc(int N, int halo, const double *phiG, const double *phi, con
  * runs as one launch per lane over a shared work list, captured in a CUDA graph. */
 int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out);
 int ccs_batch_step(ccs_batch *b, int nsteps);
+/* Same, enqueued on the batch's stream (ccs_batch_stream) without waiting. */
+int ccs_batch_step_async(ccs_batch *b, int nsteps);
+void *ccs_batch_stream(ccs_batch *b);
 void ccs_batch_destroy(ccs_batch *b);
 
 /* ---- introspection -------------------------------------------------------- */
