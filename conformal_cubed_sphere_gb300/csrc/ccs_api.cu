@@ -527,6 +527,21 @@ int ccs_sync(ccs_handle *h) {
   return CCS_OK;
 }
 
+int ccs_set_operator(ccs_handle *h, int op) {
+  if (!h) return CCS_ERR_ARG;
+  if (op != CCS_OP_WENO && op != CCS_OP_CENTRAL2 && op != CCS_OP_CENTRAL4 && op != CCS_OP_CENTRAL6)
+    return CCS_ERR_ARG;
+  if (h->cfg.precision == CCS_MIXED) return op == CCS_OP_WENO ? CCS_OK : CCS_ERR_UNSUPPORTED;
+  cudaSetDevice(h->cfg.device);
+  for (F64Stage &s : h->h_stages) s.op = op;
+  // the captured graphs read the descriptors from device memory: updating them in
+  // place (after the stream's pending steps) is all a change needs
+  CCS_TRY(h, cudaMemcpyAsync(h->d_stages, h->h_stages.data(), h->h_stages.size() * sizeof(F64Stage),
+                             cudaMemcpyHostToDevice, h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  return CCS_OK;
+}
+
 int ccs_spatial_operator(ccs_handle *h, double *tp, double *tu, double *tv) {
   if (!h) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);

@@ -98,6 +98,15 @@ __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double
   return ((0. + s0 * w0) + s1 * w1) + s2 * w2;
 }
 
+// Centred difference of cell values f[-3s .. 3s] around f[0], divided by the
+// stencil's denominator times d: spatial_operators_mod_2nd.F90:54-59,
+// spatial_operators_mod_4th.F90:58-63, spatial_operators_mod_6th.F90:62-67.
+__device__ __forceinline__ double central_diff(int op, const double *f, int s, double d) {
+  if (op == 2) return (f[s] - f[-s]) / (2. * d);
+  if (op == 4) return (f[-2 * s] - 8. * f[-s] + 8. * f[s] - f[2 * s]) / (12. * d);
+  return (-f[-3 * s] + 9. * f[-2 * s] - 45. * f[-s] + 45. * f[s] - 9. * f[2 * s] + f[3 * s]) / (60. * d);
+}
+
 struct Smem {
   // cell quantities on the halo'd tile (row-major [RY][RX])
   double phit[RN], phitG[RN], E[RN], Fx[RN], Fy[RN], uC[RN], vC[RN], ig11[RN], ig22[RN], u[RN], v[RN];
@@ -121,6 +130,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
     const int N = L.N, p = wi.panel;
     const int i0 = 1 + wi.tx * TX, j0 = 1 + wi.ty * TY;
     const int nrec = st.ediss ? 8 : 6;
+    const int op = st.op;  // uniform over the work item
 
     // ---- phase 1: cell quantities (spatial_operators_mod.F90:71-78) ----------
     for (int r = tid; r < RN; r += NT) {
@@ -150,6 +160,8 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
     __syncthreads();
 
     // ---- phase 2: face reconstructions (weno, :183-277) ---------------------
+    // (the central-difference operators have no faces: straight to phase 3)
+    if (op == CCS_OP_WENO) {
     for (int t = tid; t < nrec * NF; t += NT) {
       const int face = t % NF, q = t / NF;
       const double *fld;
@@ -219,6 +231,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
       rec[1 * NF + face] = 0.5 * (Ep + En - mx * (dn - dp));
     }
     __syncthreads();
+    }  // op == CCS_OP_WENO
 
     // ---- phase 3: tendencies, stage update, boundary correction --------------
     {
@@ -226,22 +239,31 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
       const int i = i0 + li, j = j0 + lj;
       if (i <= N && j <= N) {
         const int64_t c = L.idx(i, j, p);
-        const double *FF = rec, *EF = rec + NF;
-        const int xl = lj * (TX + 1) + li, xr = xl + 1;
-        const int yb = NFX + lj * TX + li, yt = yb + TX;
-        const double dfluxdx = (FF[xr] - FF[xl]) / st.dx;
-        const double dEdx = (EF[xr] - EF[xl]) / st.dx;
-        const double *vr = S.v + (lj + 3) * RX + li;  // v(i-3 .. i+3) at vr[0..6]
-        const double dvdx = (-vr[0] + 9. * vr[1] - 45. * vr[2] + 45. * vr[4] - 9. * vr[5] + vr[6]) / st.dx60;
-        const double dfluxdy = (FF[yt] - FF[yb]) / st.dy;
-        const double dEdy = (EF[yt] - EF[yb]) / st.dy;
-        const double *uc = S.u + lj * RX + li + 3;  // u(j-3 .. j+3) at uc[k * RX]
-        const double dudy = (-uc[0] + 9. * uc[RX] - 45. * uc[2 * RX] + 45. * uc[4 * RX] - 9. * uc[5 * RX] +
-                             uc[6 * RX]) /
-                            st.dy60;
+        const int rc = (lj + 3) * RX + li + 3;
+        double dfluxdx, dEdx, dvdx, dfluxdy, dEdy, dudy;
+        if (op == CCS_OP_WENO) {
+          const double *FF = rec, *EF = rec + NF;
+          const int xl = lj * (TX + 1) + li, xr = xl + 1;
+          const int yb = NFX + lj * TX + li, yt = yb + TX;
+          dfluxdx = (FF[xr] - FF[xl]) / st.dx;
+          dEdx = (EF[xr] - EF[xl]) / st.dx;
+          const double *vr = S.v + (lj + 3) * RX + li;  // v(i-3 .. i+3) at vr[0..6]
+          dvdx = (-vr[0] + 9. * vr[1] - 45. * vr[2] + 45. * vr[4] - 9. * vr[5] + vr[6]) / st.dx60;
+          dfluxdy = (FF[yt] - FF[yb]) / st.dy;
+          dEdy = (EF[yt] - EF[yb]) / st.dy;
+          const double *uc = S.u + lj * RX + li + 3;  // u(j-3 .. j+3) at uc[k * RX]
+          dudy = (-uc[0] + 9. * uc[RX] - 45. * uc[2 * RX] + 45. * uc[4 * RX] - 9. * uc[5 * RX] + uc[6 * RX]) /
+                 st.dy60;
+        } else {
+          dfluxdx = central_diff(op, S.Fx + rc, 1, st.dx);
+          dEdx = central_diff(op, S.E + rc, 1, st.dx);
+          dvdx = central_diff(op, S.v + rc, 1, st.dx);
+          dfluxdy = central_diff(op, S.Fy + rc, RX, st.dy);
+          dEdy = central_diff(op, S.E + rc, RX, st.dy);
+          dudy = central_diff(op, S.u + rc, RX, st.dy);
+        }
         const double sqrtG = st.m.sqrtG[c];
         const double vort = dvdx - dudy + sqrtG * st.m.f[c];
-        const int rc = (lj + 3) * RX + li + 3;
         const double uCc = S.uC[rc], vCc = S.vC[rc];
         const double tp = -(dfluxdx + dfluxdy);
         const double tu = -dEdx + vort * vCc;

@@ -37,6 +37,7 @@ struct F64Stage {
   double *tphiG, *tu, *tv;
   double dx, dy, dx60, dy60, c1;
   int kind, ediss;
+  int op;  // CCS_OP_WENO, or the central-difference order 2 / 4 / 6
 };
 
 // Mixed lane: one instance's stage launch.

@@ -170,7 +170,7 @@ class Stepper:
 
     def __init__(self, mesh: Mesh, dt: float, precision: str = "fp64", scheme: str = "RK4",
                  e_dissipation: int = L.CCS_EDISS_ZERO, device: int = 0, phi_mean: float = 0.0,
-                 share_with: "Stepper | None" = None):
+                 share_with: "Stepper | None" = None, operator: int = L.CCS_OP_WENO):
         self.mesh = mesh
         self.dt = float(dt)
         cfg = L.Config(N=mesh.N, halo=mesh.halo, scheme=L.CCS_RK4 if scheme == "RK4" else L.CCS_RK3_TVD,
@@ -186,6 +186,12 @@ class Stepper:
         else:
             L.check(lib.ccs_init_shared(C.byref(cfg), share_with.handle, C.byref(h)), "ccs_init_shared")
         self.handle = h
+        if operator != L.CCS_OP_WENO:
+            self.set_operator(operator)
+
+    def set_operator(self, op: int):
+        """The spatial operator (CCS_OP_WENO or CCS_OP_CENTRAL2/4/6), FP64 lane."""
+        L.check(L.lib().ccs_set_operator(self.handle, int(op)), "ccs_set_operator", self.handle)
 
     def close(self):
         if self.handle:

@@ -63,6 +63,13 @@ enum {
  * RECONSTRUCT fills them with WENO reconstructions of u at x-faces and v at y-faces. */
 enum { CCS_EDISS_ZERO = 0, CCS_EDISS_RECONSTRUCT = 1 };
 
+/* spatial operator.  The reference ships four interchangeable modules of the same
+ * name and compiles one of them: spatial_operators_mod.F90 (WENO-Z reconstruction
+ * with Rusanov face fluxes, the default) and the centred-difference modules
+ * spatial_operators_mod_2nd.F90, _4th.F90 and _6th.F90.  The CENTRAL values are the
+ * order of accuracy. */
+enum { CCS_OP_WENO = 0, CCS_OP_CENTRAL2 = 2, CCS_OP_CENTRAL4 = 4, CCS_OP_CENTRAL6 = 6 };
+
 /* cube-to-sphere map used by the host mesh generator: the conformal cubic map of
  * the reference mesh generator (gen_method 'Rancic', mesh_generation/src/
  * mesh_mod.f90:150-171) or the equiangular gnomonic map */
@@ -141,6 +148,13 @@ int ccs_step(ccs_handle *h, int nsteps);
 /* Same, enqueued on the handle's stream; ccs_sync waits for it. */
 int ccs_step_async(ccs_handle *h, int nsteps);
 int ccs_sync(ccs_handle *h);
+
+/* Selects the spatial operator of the handle's steps (default CCS_OP_WENO): the
+ * choice the reference makes at build time by compiling one of its four
+ * spatial_operators_mod sources.  FP64 lane only (CCS_ERR_UNSUPPORTED on the mixed
+ * lane for anything but CCS_OP_WENO); a batch copies its members' operators when
+ * it is created.  No counterpart call in the reference. */
+int ccs_set_operator(ccs_handle *h, int op);
 
 /* spatial_operator(stat(old), tend) (spatial_operators_mod.F90:13-181): the
  * tendencies of phiG, u, v of the current state, interior cells (halo and corner

@@ -17,6 +17,11 @@
  * with no contraction (build with -ffp-contract=off): the reference is built with
  * -fdefault-real-8 and, on x86-64 without -march, gfortran emits no FMA.
  *
+ * The spatial operator is the WENO-Z/Rusanov one of spatial_operators_mod.F90 by
+ * default; orc_set_operator selects the central-difference modules
+ * spatial_operators_mod_{2nd,4th,6th}.F90 instead (the reference picks one of them
+ * at build time).
+ *
  * Array layout is the reference's: Fortran column-major (i, j, panel) with
  * i, j in [1-h, N+h], panel in [1, 6]; 2x2 matrices (2,2,i,j,panel); the Jacobian
  * (3,2,i,j,panel); extended face arrays (2N+1, 2N+1, 6).
@@ -50,6 +55,7 @@ typedef struct orc_ctx {
   size_t ncell, next;
   double dx, dy;
   int e_diss; /* 0: never-written u/v face slots read as 0.0; 1: reconstructed */
+  int op;     /* spatial operator: 0 WENO-Z/Rusanov, 2/4/6 central differences */
   /* mesh (owned copies) */
   double *sqrtG, *G, *IG, *A, *IA, *f, *phis;
   /* stat(-4:1), tend(-4:1): index = slot + 4 */
@@ -531,6 +537,15 @@ void orc_destroy(orc_ctx *c) {
 
 void orc_set_e_dissipation(orc_ctx *c, int mode) { c->e_diss = mode; }
 
+/* 0 selects spatial_operators_mod.F90 (WENO-Z + Rusanov); 2, 4 and 6 select the
+   central-difference modules spatial_operators_mod_{2nd,4th,6th}.F90.  Returns 0,
+   or -1 for any other value (the operator is left unchanged). */
+int orc_set_operator(orc_ctx *c, int op) {
+  if (op != 0 && op != 2 && op != 4 && op != 6) return -1;
+  c->op = op;
+  return 0;
+}
+
 static orc_state *slot_state(orc_ctx *c, int slot) { return &c->stat[slot + 4]; }
 static orc_tend *slot_tend(orc_ctx *c, int slot) { return &c->tend[slot + 4]; }
 
@@ -558,7 +573,53 @@ void orc_get_tend(orc_ctx *c, int slot, int id, double *dst) {
 /* ------------------------------------------------------------------------- */
 /* spatial_operator: spatial_operators_mod.F90:13-181                         */
 /* ------------------------------------------------------------------------- */
+/* Central-difference operators: spatial_operators_mod_2nd.F90:13-70,
+   spatial_operators_mod_4th.F90:13-74, spatial_operators_mod_6th.F90:13-81.
+   Same prologue as the WENO operator (:38-45 there), then every derivative is a
+   centred difference of the cell values, evaluated left to right as written. */
+static double cd_diff(int op, const double *f, size_t k, ptrdiff_t s, double d) {
+  if (op == 2) return (f[k + s] - f[k - s]) / (2. * d);
+  if (op == 4) return (f[k - 2 * s] - 8. * f[k - s] + 8. * f[k + s] - f[k + 2 * s]) / (12. * d);
+  return (-f[k - 3 * s] + 9. * f[k - 2 * s] - 45. * f[k - s] + 45. * f[k + s] - 9. * f[k + 2 * s] + f[k + 3 * s]) /
+         (60. * d);
+}
+
+static void spatial_operator_cd(orc_ctx *c, const orc_state *st, orc_tend *td) {
+  const int N = c->N, op = c->op;
+  const size_t n = c->ncell;
+  const ptrdiff_t sx = 1, sy = c->nh;
+#pragma omp parallel for schedule(static)
+  for (size_t k = 0; k < n; k++) {
+    c->phit[k] = st->phi[k] + c->phis[k];
+    c->K[k] = 0.5 * (st->u[k] * st->uC[k] + st->v[k] * st->vC[k]);
+    c->E[k] = c->phit[k] + c->K[k];
+    c->flux_x[k] = st->phiG[k] * st->uC[k];
+    c->flux_y[k] = st->phiG[k] * st->vC[k];
+  }
+  for (int p = 1; p <= 6; p++) {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= N; j++)
+      for (int i = 1; i <= N; i++) {
+        const size_t k = CI(c, i, j, p);
+        c->dfluxdx[k] = cd_diff(op, c->flux_x, k, sx, c->dx);
+        c->dEdx[k] = cd_diff(op, c->E, k, sx, c->dx);
+        c->dvdx[k] = cd_diff(op, st->v, k, sx, c->dx);
+        c->dfluxdy[k] = cd_diff(op, c->flux_y, k, sy, c->dy);
+        c->dEdy[k] = cd_diff(op, c->E, k, sy, c->dy);
+        c->dudy[k] = cd_diff(op, st->u, k, sy, c->dy);
+        c->vort[k] = c->dvdx[k] - c->dudy[k] + c->sqrtG[k] * c->f[k];
+        td->phiG[k] = -(c->dfluxdx[k] + c->dfluxdy[k]);
+        td->u[k] = -c->dEdx[k] + c->vort[k] * st->vC[k];
+        td->v[k] = -c->dEdy[k] - c->vort[k] * st->uC[k];
+      }
+  }
+}
+
 static void spatial_operator(orc_ctx *c, const orc_state *st, orc_tend *td) {
+  if (c->op != 0) {
+    spatial_operator_cd(c, st, td);
+    return;
+  }
   const int N = c->N;
   const size_t n = c->ncell;
   const double dx = c->dx, dy = c->dy;

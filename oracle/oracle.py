@@ -39,6 +39,7 @@ def lib() -> C.CDLL:
             "orc_set_threads": (None, [C.c_int]),
             "orc_get_threads": (C.c_int, []),
             "orc_set_e_dissipation": (None, [C.c_void_p, C.c_int]),
+            "orc_set_operator": (C.c_int, [C.c_void_p, C.c_int]),
             "orc_set_field": (None, [C.c_void_p, C.c_int, C.c_int, _dp]),
             "orc_get_field": (None, [C.c_void_p, C.c_int, C.c_int, _dp]),
             "orc_get_tend": (None, [C.c_void_p, C.c_int, C.c_int, _dp]),
@@ -104,7 +105,7 @@ class Oracle:
     """The reference step on the CPU: stat(0) -> stat(1) by RK4 / RK3_TVD."""
 
     def __init__(self, N, halo, dx, dy, sqrtG, matrixG, matrixIG, matrixA, matrixIA, f, phis,
-                 e_dissipation: int = 0, threads: int = 0):
+                 e_dissipation: int = 0, threads: int = 0, operator: int = 0):
         L = lib()
         if threads:
             L.orc_set_threads(int(threads))
@@ -114,6 +115,8 @@ class Oracle:
         if not self.ctx:
             raise ValueError("oracle: bad sizes")
         L.orc_set_e_dissipation(self.ctx, int(e_dissipation))
+        if L.orc_set_operator(self.ctx, int(operator)) != 0:
+            raise ValueError(f"oracle: unknown spatial operator {operator}")
         self.N, self.halo = N, halo
         self.ncell = (N + 2 * halo) ** 2 * 6
 

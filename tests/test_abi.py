@@ -104,3 +104,7 @@ def test_streamfunction_winds_are_nondivergent():
            (u[h:h + N, h + 1:h + N + 1] - u[h:h + N, h - 1:h + N - 1]) / (2 * mesh.dy)
     inner = (slice(4, N - 4), slice(4, N - 4))
     assert np.max(np.abs(div[inner])) < 0.05 * np.max(np.abs(vort[inner]))
+
+
+def test_set_operator_rejects_null_handle_without_device():
+    assert L.lib().ccs_set_operator(None, L.CCS_OP_CENTRAL4) == L.CCS_ERR_ARG

@@ -168,3 +168,51 @@ def test_constant_division_is_correctly_rounded(b):
     assert rc == 0
     assert np.array_equal(fast.view(np.int64), ieee.view(np.int64))
     assert np.array_equal(ieee, x / b)
+
+
+@pytest.mark.parametrize("op", [L.CCS_OP_CENTRAL2, L.CCS_OP_CENTRAL4, L.CCS_OP_CENTRAL6])
+def test_central_difference_operator_bitwise(op):
+    """spatial_operators_mod_{2nd,4th,6th}.F90: tendency and 5 RK4 steps bit for bit."""
+    mesh, s, dt = seeded_case(20, 3, seed=5, oro=True)
+    gpu = M.Stepper(mesh, 0.5 * dt, precision="fp64", operator=op)
+    gpu.set_state(s)
+    orc = O.Oracle.from_mesh(mesh, operator=op)
+    orc.set_state(s.arrays)
+    im = mesh.interior_mask()
+    for a, b in zip(gpu.spatial_operator(), orc.spatial_operator()):
+        assert bitwise_equal(a, b, im), max_rel(a, b, im)
+    gpu.step(5)
+    orc.run(0.5 * dt, 5)
+    g, o = gpu.get_state(), orc.get_state()
+    m = valid_mask(mesh)
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(g[k], o[k], m), (k, max_rel(g[k], o[k], m))
+
+
+def test_operator_switch_and_batch_carry_the_operator():
+    """Switching a handle's operator takes effect on its next step; a batch built
+    afterwards steps each member with its own operator (RK3_TVD member included)."""
+    mesh, s, dt = seeded_case(16, 3, seed=9, oro=False)
+    a = M.Stepper(mesh, dt, precision="fp64")
+    a.set_operator(L.CCS_OP_CENTRAL4)
+    b = M.Stepper(mesh, dt, precision="fp64", scheme="RK3_TVD", operator=L.CCS_OP_CENTRAL2)
+    c = M.Stepper(mesh, dt, precision="fp64")  # WENO
+    for x in (a, b, c):
+        x.set_state(s)
+    M.Batch([a, b, c]).step(3)
+    m = valid_mask(mesh)
+    for stepper, op, scheme in ((a, 4, "RK4"), (b, 2, "RK3_TVD"), (c, 0, "RK4")):
+        orc = O.Oracle.from_mesh(mesh, operator=op)
+        orc.set_state(s.arrays)
+        orc.run(dt, 3, scheme)
+        g, o = stepper.get_state(), orc.get_state()
+        for k in CHECK_FIELDS:
+            assert bitwise_equal(g[k], o[k], m), (op, k, max_rel(g[k], o[k], m))
+
+
+def test_mixed_lane_rejects_central_operators():
+    mesh, s, dt = seeded_case(8, 3, oro=False)
+    x = M.Stepper(mesh, dt, precision="mixed", phi_mean=8000.0 * mesh.gravity)
+    x.set_operator(L.CCS_OP_WENO)
+    with pytest.raises(L.CCSError):
+        x.set_operator(L.CCS_OP_CENTRAL4)
