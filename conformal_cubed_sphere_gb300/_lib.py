@@ -20,6 +20,7 @@ CCS_ERR_MESH = 6
 CCS_ERR_NOMEM = 7
 CCS_ERR_NODEVICE = 8
 CCS_ERR_TOO_LARGE = 9
+CCS_ERR_IO = 10
 CCS_NOALLOC_MAX_N = 4096
 
 CCS_RK4 = 0
@@ -94,6 +95,9 @@ SIGNATURES = {
     "ccs_stream": (C.c_void_p, [_vp]),
     "ccs_selftest_div": (C.c_int, [_dp, C.c_int64, C.c_double, _dp, _dp]),
     "ccs_strerror": (C.c_char_p, [C.c_int]),
+    "ccs_mesh_save": (C.c_int, [C.c_char_p, C.c_int, C.c_int] + [_dp] * 6),
+    "ccs_mesh_file_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "ccs_mesh_load": (C.c_int, [C.c_char_p, C.c_int] + [_dp] * 6),
     "ccs_last_error": (C.c_char_p, [_vp]),
     "ccs_abi_version": (C.c_int, []),
     "ccs_mesh_generate": (C.c_int, [C.c_int, C.c_int] + [_dp] * 6),

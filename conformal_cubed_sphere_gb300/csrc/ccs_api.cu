@@ -371,6 +371,7 @@ const char *ccs_strerror(int status) {
     case CCS_ERR_NOMEM: return "out of memory";
     case CCS_ERR_NODEVICE: return "no CUDA device";
     case CCS_ERR_TOO_LARGE: return "size exceeds the fixed scratch capacity";
+    case CCS_ERR_IO: return "mesh file missing, unreadable or not in the raw mesh format";
     default: return "unknown status";
   }
 }

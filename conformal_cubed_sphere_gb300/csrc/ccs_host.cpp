@@ -7,6 +7,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -941,4 +942,93 @@ extern "C" double ccs_cfl_dt(int N, int halo, double cfl, double dx, double dy, 
       }
   if (!(lmax > 0.)) return -1.;
   return cfl * (dx < dy ? dx : dy) / lmax;
+}
+
+// ---- raw-binary mesh file --------------------------------------------------------
+// A stand-in for the NetCDF mesh file of mesh_generation/src/output_mod.f90:25-86 and
+// read_mesh (io_mod.F90:36-101), for machines without libnetcdf.  It holds the
+// global attributes read_mesh reads (dx, dy in degrees; ids, ide, jds, jde, ifs,
+// ife) and the cell-centre samples of lon, lat, x, y, z and jab that the time step
+// uses, little-endian, Fortran order:
+//   bytes  0-7   magic "CCSMESH" + '\1'
+//          8-47  int32 version (1), N, map, ids, ide, jds, jde, ifs, ife, reserved (0)
+//         48-63  float64 dx, dy (degrees)
+//         64-    float64 lon, lat, x, y, z (N, N, 6) then jab (3, 2, N, N, 6)
+namespace {
+
+const char kMeshMagic[8] = {'C', 'C', 'S', 'M', 'E', 'S', 'H', '\1'};
+constexpr int kMeshHeader = 64;
+
+struct MeshHeader {
+  int32_t version, N, map, ids, ide, jds, jde, ifs, ife, reserved;
+  double dx, dy;
+};
+
+int read_mesh_header(FILE *fp, MeshHeader *hd) {
+  char magic[8];
+  if (fread(magic, 1, 8, fp) != 8 || std::memcmp(magic, kMeshMagic, 8) != 0) return CCS_ERR_IO;
+  int32_t iv[10];
+  double dv[2];
+  if (fread(iv, sizeof(int32_t), 10, fp) != 10 || fread(dv, sizeof(double), 2, fp) != 2) return CCS_ERR_IO;
+  hd->version = iv[0]; hd->N = iv[1]; hd->map = iv[2];
+  hd->ids = iv[3]; hd->ide = iv[4]; hd->jds = iv[5]; hd->jde = iv[6]; hd->ifs = iv[7]; hd->ife = iv[8];
+  hd->reserved = iv[9];
+  hd->dx = dv[0]; hd->dy = dv[1];
+  // version 1 only; the index attributes must describe the (2N+1)^2 x 6 grid
+  if (hd->version != 1 || hd->N < 1 || hd->N > 8192) return CCS_ERR_IO;
+  if (hd->ids != 1 || hd->jds != 1 || hd->ide != 2 * hd->N + 1 || hd->jde != 2 * hd->N + 1 || hd->ifs != 1 ||
+      hd->ife != 6)
+    return CCS_ERR_IO;
+  return CCS_OK;
+}
+
+}  // namespace
+
+extern "C" int ccs_mesh_save(const char *path, int N, int map, const double *lon_deg, const double *lat_deg,
+                             const double *x, const double *y, const double *z, const double *jab) {
+  if (!path || N < 1 || N > 8192 || !lon_deg || !lat_deg || !x || !y || !z || !jab) return CCS_ERR_ARG;
+  FILE *fp = std::fopen(path, "wb");
+  if (!fp) return CCS_ERR_IO;
+  const int32_t iv[10] = {1, N, map, 1, 2 * N + 1, 1, 2 * N + 1, 1, 6, 0};
+  const double dv[2] = {90. / N, 90. / N};
+  const size_t n = (size_t)N * N * 6;
+  bool ok = std::fwrite(kMeshMagic, 1, 8, fp) == 8 && std::fwrite(iv, sizeof(int32_t), 10, fp) == 10 &&
+            std::fwrite(dv, sizeof(double), 2, fp) == 2;
+  const double *arr[5] = {lon_deg, lat_deg, x, y, z};
+  for (int k = 0; k < 5 && ok; k++) ok = std::fwrite(arr[k], sizeof(double), n, fp) == n;
+  if (ok) ok = std::fwrite(jab, sizeof(double), 6 * n, fp) == 6 * n;
+  if (std::fclose(fp) != 0) ok = false;
+  return ok ? CCS_OK : CCS_ERR_IO;
+}
+
+extern "C" int ccs_mesh_file_info(const char *path, int *N, int *map) {
+  if (!path || !N) return CCS_ERR_ARG;
+  FILE *fp = std::fopen(path, "rb");
+  if (!fp) return CCS_ERR_IO;
+  MeshHeader hd{};
+  const int rc = read_mesh_header(fp, &hd);
+  std::fclose(fp);
+  if (rc) return rc;
+  *N = hd.N;
+  if (map) *map = hd.map;
+  return CCS_OK;
+}
+
+extern "C" int ccs_mesh_load(const char *path, int N, double *lon_deg, double *lat_deg, double *x, double *y,
+                             double *z, double *jab) {
+  if (!path || N < 1 || !lon_deg || !lat_deg || !x || !y || !z || !jab) return CCS_ERR_ARG;
+  FILE *fp = std::fopen(path, "rb");
+  if (!fp) return CCS_ERR_IO;
+  MeshHeader hd{};
+  int rc = read_mesh_header(fp, &hd);
+  if (!rc && hd.N != N) rc = CCS_ERR_ARG;
+  if (!rc && std::fseek(fp, kMeshHeader, SEEK_SET) != 0) rc = CCS_ERR_IO;
+  const size_t n = (size_t)N * N * 6;
+  double *arr[5] = {lon_deg, lat_deg, x, y, z};
+  for (int k = 0; k < 5 && !rc; k++)
+    if (std::fread(arr[k], sizeof(double), n, fp) != n) rc = CCS_ERR_IO;
+  if (!rc && std::fread(jab, sizeof(double), 6 * n, fp) != 6 * n) rc = CCS_ERR_IO;
+  if (!rc && std::fgetc(fp) != EOF) rc = CCS_ERR_IO;  // trailing bytes: not this format
+  std::fclose(fp);
+  return rc;
 }

@@ -38,21 +38,33 @@ class Mesh:
     """Metric arrays of an N x N x 6 cubed sphere with `halo` ghost cells."""
 
     def __init__(self, N: int, halo: int = 3, radius: float = RADIUS, omega: float = OMEGA,
-                 gravity: float = GRAVITY, phis: np.ndarray | None = None, cube_map: str = "conformal"):
+                 gravity: float = GRAVITY, phis: np.ndarray | None = None, cube_map: str = "conformal",
+                 mesh_file: str | None = None):
+        lib = L.lib()
+        if mesh_file is not None:
+            fn, fmap = C.c_int(), C.c_int()
+            L.check(lib.ccs_mesh_file_info(str(mesh_file).encode(), C.byref(fn), C.byref(fmap)),
+                    "ccs_mesh_file_info")
+            N = fn.value
+            cube_map = {L.CCS_MAP_CONFORMAL: "conformal", L.CCS_MAP_GNOMONIC_EQUIANGULAR: "gnomonic"}.get(
+                fmap.value, "file")
         self.N, self.halo = int(N), int(halo)
         self.cube_map = cube_map
         self.radius, self.omega, self.gravity = float(radius), float(omega), float(gravity)
         self.nh = self.N + 2 * self.halo
         self.ncell = self.nh * self.nh * 6
-        lib = L.lib()
         n = self.N * self.N * 6
         self.file = {k: np.zeros(n) for k in ("lon", "lat", "x", "y", "z")}
         self.file["jab"] = np.zeros(6 * n)
         f = self.file
-        kind = {"conformal": L.CCS_MAP_CONFORMAL, "gnomonic": L.CCS_MAP_GNOMONIC_EQUIANGULAR}[cube_map]
-        L.check(lib.ccs_mesh_generate(self.N, kind, _ptr(f["lon"]), _ptr(f["lat"]),
-                                      _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"])),
-                "ccs_mesh_generate")
+        if mesh_file is not None:
+            L.check(lib.ccs_mesh_load(str(mesh_file).encode(), self.N, _ptr(f["lon"]), _ptr(f["lat"]),
+                                      _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"])), "ccs_mesh_load")
+        else:
+            kind = {"conformal": L.CCS_MAP_CONFORMAL, "gnomonic": L.CCS_MAP_GNOMONIC_EQUIANGULAR}[cube_map]
+            L.check(lib.ccs_mesh_generate(self.N, kind, _ptr(f["lon"]), _ptr(f["lat"]),
+                                          _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"])),
+                    "ccs_mesh_generate")
         nc = self.ncell
         self.sqrtG = np.zeros(nc)
         self.matrixG = np.zeros(4 * nc)
@@ -73,6 +85,20 @@ class Mesh:
         self.dx = (90.0 / self.N) * D2R
         self.dy = self.dx
         self.phis = np.zeros(nc) if phis is None else np.ascontiguousarray(phis, dtype=np.float64)
+
+    @classmethod
+    def from_file(cls, path, halo: int = 3, **kw) -> "Mesh":
+        """The mesh of a raw-binary mesh file (ccs_mesh_load), metric derived as
+        read_mesh does (io_mod.F90:119-306)."""
+        return cls(0, halo, mesh_file=path, **kw)
+
+    def save(self, path) -> None:
+        """Writes the generator samples as a raw-binary mesh file (ccs_mesh_save);
+        Mesh(mesh_file=path, halo=...) reads it back."""
+        f = self.file
+        kind = {"conformal": L.CCS_MAP_CONFORMAL, "gnomonic": L.CCS_MAP_GNOMONIC_EQUIANGULAR}.get(self.cube_map, -1)
+        L.check(L.lib().ccs_mesh_save(str(path).encode(), self.N, kind, _ptr(f["lon"]), _ptr(f["lat"]),
+                                      _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"])), "ccs_mesh_save")
 
     def view(self) -> L.MeshView:
         mv = L.MeshView()

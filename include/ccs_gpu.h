@@ -44,7 +44,8 @@ enum {
   CCS_ERR_MESH = 6,        /* singular metric (io_mod.F90:176-188 stops here) */
   CCS_ERR_NOMEM = 7,       /* device or host allocation failed */
   CCS_ERR_NODEVICE = 8,    /* no CUDA device visible */
-  CCS_ERR_TOO_LARGE = 9    /* size above a fixed capacity (ccs_diag_noalloc) */
+  CCS_ERR_TOO_LARGE = 9,   /* size above a fixed capacity (ccs_diag_noalloc) */
+  CCS_ERR_IO = 10          /* mesh file missing, unreadable, truncated or not in this format */
 };
 
 /* integral_scheme (parameters_mod.F90:402-408) */
@@ -229,6 +230,22 @@ int ccs_abi_version(void);
  * mesh_generation/src/cuco.f90:17-36. */
 int ccs_mesh_generate(int N, int map, double *lon_deg, double *lat_deg, double *x,
                       double *y, double *z, double *jab);
+
+/* Raw-binary mesh file, for machines without libnetcdf: the global attributes that
+ * read_mesh takes from the NetCDF mesh file (io_mod.F90:36-47: dx, dy in degrees,
+ * ids, ide, jds, jde, ifs, ife) and the cell-centre samples of its lon, lat, x, y, z
+ * and jab variables (:87-101), little-endian, Fortran order, in the layout of
+ * ccs_mesh_generate.  Header: 8-byte magic "CCSMESH\1", ten int32 (version 1, N, map,
+ * ids, ide, jds, jde, ifs, ife, 0), two float64 (dx, dy); then lon, lat, x, y, z
+ * (N*N*6 float64 each) and jab (6*N*N*6).  ccs_mesh_file_info reads N (and the map
+ * id, if map is non-NULL) so the caller can size the arrays for ccs_mesh_load;
+ * ccs_mesh_load fails with CCS_ERR_ARG when the file's N differs from N, and with
+ * CCS_ERR_IO on a missing, short, over-long or foreign file. */
+int ccs_mesh_save(const char *path, int N, int map, const double *lon_deg, const double *lat_deg,
+                  const double *x, const double *y, const double *z, const double *jab);
+int ccs_mesh_file_info(const char *path, int *N, int *map);
+int ccs_mesh_load(const char *path, int N, double *lon_deg, double *lat_deg, double *x, double *y,
+                  double *z, double *jab);
 
 /* io_mod.F90:119-220, 295-306: halo fill of the samples and per-cell G = J^T J,
  * G^-1, sqrt(det G), A = S J, A^-1 (pole cases included), f = 2 Omega sin(lat).
