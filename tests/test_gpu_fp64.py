@@ -216,3 +216,16 @@ def test_mixed_lane_rejects_central_operators():
     x.set_operator(L.CCS_OP_WENO)
     with pytest.raises(L.CCSError):
         x.set_operator(L.CCS_OP_CENTRAL4)
+
+
+def test_c192_1000_steps_with_orography_bitwise():
+    """Long-run configuration: C192, halo 3, FP64, RK4, 1000 steps at CFL 0.5 over
+    seeded orography (about 1.5 simulated days).  The oracle takes one to three
+    minutes on the host cores; the lane must stay bit for bit on every checked field."""
+    mesh, s, dt, gpu, orc = _pair(192, 3, seed=1, oro=True)
+    gpu.step(1000)
+    orc.run(dt, 1000)
+    g, o = gpu.get_state(), orc.get_state()
+    m = valid_mask(mesh)
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(g[k], o[k], m), (k, max_rel(g[k], o[k], m))
