@@ -1,0 +1,98 @@
+"""The model program's time loop (ccsm.F90:40-63) around the GPU step: output
+times, step counts and the MCR/ECR records."""
+import pytest
+
+from conformal_cubed_sphere_gb300 import driver as D
+
+
+def test_default_time_settings_follow_the_namelist_defaults():
+    ts = D.TimeSettings()
+    assert (ts.dt, ts.total_run_time, ts.nsteps, ts.history_interval) == (300.0, 86400, 288, 360)
+    assert ts.total_output_num == 240
+    # mod(it*300, 360) == 0 only every sixth step: 48 outputs, the last at the end
+    steps = D.output_steps(ts)
+    assert steps == list(range(6, 289, 6))
+
+
+def test_output_times_in_double_precision():
+    ts = D.TimeSettings(dt=600.0, run_days=0, run_hours=6, history_interval=3600)
+    assert ts.nsteps == 36 and D.output_steps(ts) == [6, 12, 18, 24, 30, 36]
+    # a dt that never lands on the interval writes nothing, as the reference would
+    ts = D.TimeSettings(dt=7.3, run_days=0, run_hours=1, history_interval=600)
+    assert ts.nsteps == int(3600 / 7.3)
+    assert D.output_steps(ts) == [it for it in range(1, ts.nsteps + 1) if (it * 7.3) % 600.0 == 0.0]
+
+
+def test_truncating_step_count():
+    ts = D.TimeSettings(dt=700.0, run_days=0, run_hours=1)
+    assert ts.nsteps == 5  # 3600 / 700 = 5.14 -> 5
+
+
+class _FakeStepper:
+    """Counts steps; diag returns (mass, energy) as functions of the step count."""
+
+    def __init__(self):
+        self.n = 0
+        self.calls = []
+
+    def step(self, k):
+        assert k >= 1
+        self.n += k
+        self.calls.append(k)
+
+    def diag(self):
+        return 100.0 + self.n, 1000.0 + 2 * self.n
+
+    def get_state(self):
+        return self.n
+
+
+def test_run_chunks_steps_and_uses_old_state_energy():
+    ts = D.TimeSettings(dt=600.0, run_days=0, run_hours=2, history_interval=1800)
+    f = _FakeStepper()
+    seen = []
+    recs = D.run(f, ts, on_output=lambda idx, st: seen.append((idx, st)), log=None)
+    assert f.n == ts.nsteps == 12
+    assert [r.step for r in recs] == [3, 6, 9, 12]
+    assert seen == [(1, 0), (2, 3), (3, 6), (4, 9), (5, 12)]
+    # mass of the output state, energy of the state one step earlier
+    assert recs[0].mcr == pytest.approx(3 / 100.0)
+    assert recs[0].ecr == pytest.approx(2 * 2 / 1000.0)
+    g = _FakeStepper()
+    recs = D.run(g, ts, energy_of_new_state=True, log=None)
+    assert recs[0].ecr == pytest.approx(2 * 3 / 1000.0)
+    assert g.calls == [3, 3, 3, 3]
+
+
+def test_unknown_scheme_rejected():
+    with pytest.raises(ValueError):
+        D.run(_FakeStepper(), D.TimeSettings(integral_scheme="Euler"), log=None)
+
+
+@pytest.mark.gpu
+def test_driver_on_the_gpu_matches_stepping_by_hand():
+    import numpy as np
+
+    from conformal_cubed_sphere_gb300 import model as M
+    from tests.helpers import seeded_case
+
+    mesh, s, dt = seeded_case(12, 3, oro=True)
+    dt = float(int(dt))  # whole seconds, as namelist settings are
+    ts = D.TimeSettings(dt=dt, run_days=0, run_hours=0, run_minutes=0, run_seconds=int(12 * dt),
+                        history_interval=int(4 * dt))
+    a = M.Stepper(mesh, dt, precision="fp64")
+    a.set_state(s)
+    states = {}
+    recs = D.run(a, ts, on_output=lambda idx, st: states.__setitem__(idx, st), log=None)
+    b = M.Stepper(mesh, dt, precision="fp64")
+    b.set_state(s)
+    m0, e0 = b.diag()
+    for r in recs:
+        b.step(r.step - 1 - (0 if r.output_idx == 2 else recs[r.output_idx - 3].step))
+        e_old = b.diag()[1]
+        b.step(1)
+        m_new = b.diag()[0]
+        assert r.mcr == (m_new - m0) / m0 and r.ecr == (e_old - e0) / e0
+        got = b.get_state()
+        for k in ("phiG", "u", "v"):
+            assert np.array_equal(states[r.output_idx][k], got[k])
