@@ -248,6 +248,7 @@ def run_ensemble(args, torch):
                          for k in range(1, n)]
     for st, m in zip(states, members):
         m.set_state(st)
+        m.autotune(reps=5)  # timed once for the grid, then the cached choice
     batch = M.Batch(members)
     batch.step(max(args.warmup, 3))
     t_batch = _batch_time(batch, torch, args.steps)
@@ -282,6 +283,7 @@ def run_uneven(args, torch):
     from conformal_cubed_sphere_gb300 import model as M
     groups = [(48, 16), (96, 8), (192, 4), (384, 1)]
     members, cells64, cells32, k = [], 0, 0, 0
+    variants = {}
     for N, cnt in groups:
         mesh = M.Mesh(N, HALO)
         for c in range(cnt):
@@ -290,6 +292,8 @@ def run_uneven(args, torch):
             dt = M.cfl_dt(mesh, st, 0.5)
             m = M.Stepper(mesh, dt, precision=lane, phi_mean=8000.0 * mesh.gravity)
             m.set_state(st)
+            m.autotune(reps=3)  # per resolution and lane (cached after the first member)
+            variants[f"C{N}_{lane}"] = "x".join(str(t) for t in m.variant[1:])
             members.append(m)
             if lane == "fp64":
                 cells64 += 6 * N * N
@@ -307,6 +311,7 @@ def run_uneven(args, torch):
         "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 mixed + f64", "data": "synthetic (seeded spherical harmonics)",
         "config": {"workload": "29 instances, per-instance CFL dt, one FP64 member per resolution below C384",
+                   "tiles": variants,
                    "fp64_cells": cells64, "mixed_cells": cells32, "l2": "inputs larger than L2"},
         "hbm": {"alg_GBs": alg, "peak": _peaks()[0], "frac": alg / _peaks()[0]},
     }))
@@ -346,6 +351,7 @@ def main():
     phibar = 8000.0 * mesh.gravity
     mixed = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
     mixed.set_state(s)
+    tuned = {"mixed": mixed.autotune(reps=5)}
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
     mixed.step(max(args.warmup, 3))
     torch.cuda.synchronize()
@@ -374,6 +380,7 @@ def main():
     # FP64 parity lane on the same state
     f64 = M.Stepper(mesh, dt, precision="fp64", device=local)
     f64.set_state(s)
+    tuned["fp64"] = f64.autotune(reps=2)
     f64.step(1)
     torch.cuda.synchronize()
     t_f64 = time_device_steps(f64, torch, args.fp64_steps, flush)
@@ -384,6 +391,7 @@ def main():
     e2e_steps = max(3, min(20, args.steps))
     mixed2 = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
     mixed2.set_state(s)
+    mixed2.autotune()  # the cached choice
     e2e, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
 
     if rank != 0:
@@ -396,7 +404,8 @@ def main():
         "data": "synthetic (seeded spherical harmonics)",
         "config": {"workload": f"C{mesh.N} seeded state with orography, RK4, CFL 0.5, mixed FP32/FP64 lane",
                    "N": mesh.N, "halo": HALO, "dt_s": dt, "l2": "flushed (256 MB write) between timed steps",
-                   "parallelism": "replicas" if ws > 1 else "single"},
+                   "parallelism": "replicas" if ws > 1 else "single",
+                   "tile_variants": {lane: {"chosen": v, "launch_us": t} for lane, (v, t) in tuned.items()}},
         "fp64_lane": {"value": fp64_value, "unit": "cell-steps/s", "ms_per_step": 1e3 * t_f64 / args.fp64_steps,
                       "kernel_ms_avg": avg64_ms, "mixed_over_fp64": value / ws / fp64_value},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

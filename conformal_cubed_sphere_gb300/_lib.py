@@ -29,6 +29,7 @@ CCS_FP64 = 0
 CCS_MIXED = 1
 CCS_EDISS_ZERO = 0
 CCS_EDISS_RECONSTRUCT = 1
+CCS_MAX_VARIANTS = 4
 CCS_OP_WENO, CCS_OP_CENTRAL2, CCS_OP_CENTRAL4, CCS_OP_CENTRAL6 = 0, 2, 4, 6
 CCS_MAP_GNOMONIC_EQUIANGULAR = 0
 CCS_MAP_CONFORMAL = 1
@@ -83,6 +84,9 @@ SIGNATURES = {
     "ccs_sync": (C.c_int, [_vp]),
     "ccs_spatial_operator": (C.c_int, [_vp, _dp, _dp, _dp]),
     "ccs_set_operator": (C.c_int, [_vp, C.c_int]),
+    "ccs_autotune": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_int), _dp]),
+    "ccs_set_variant": (C.c_int, [_vp, C.c_int]),
+    "ccs_get_variant": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "ccs_diag": (C.c_int, [_vp, _dp, _dp]),
     "ccs_diag_noalloc": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 9 + [_vp]),
     "ccs_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),

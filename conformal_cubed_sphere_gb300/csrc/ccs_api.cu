@@ -5,8 +5,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "ccs_internal.h"
@@ -72,6 +75,7 @@ struct ccs_handle {
   WorkItem *d_work = nullptr;
   int nwork = 0;
   int grid = 0;
+  int var = 0;  // tile variant of the FP64 stage kernel (kF64Tiles)
   bool sphere_valid = false;
   cudaGraphExec_t g_step = nullptr, g_step_sw = nullptr;
   // timing
@@ -191,6 +195,25 @@ static int build_mesh(ccs_handle *h, const ccs_mesh_view *mv) {
   return CCS_OK;
 }
 
+// (Re)builds a work list of all tiles of the six panels for tile shape ts.
+static int build_work(ccs_handle *h, TileShape ts, WorkItem **d_work, int *nwork) {
+  const int N = h->L.N;
+  const int ntx = (N + ts.tx - 1) / ts.tx, nty = (N + ts.ty - 1) / ts.ty;
+  std::vector<WorkItem> work;
+  for (int p = 0; p < 6; p++)
+    for (int ty = 0; ty < nty; ty++)
+      for (int tx = 0; tx < ntx; tx++) work.push_back(WorkItem{0, (int16_t)p, (int16_t)tx, (int16_t)ty});
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  if (*d_work) CCS_TRY(h, cudaFree(*d_work));
+  *d_work = nullptr;
+  CCS_TRY(h, cudaMalloc(d_work, work.size() * sizeof(WorkItem)));
+  CCS_TRY(h, cudaMemcpyAsync(*d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                             h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  *nwork = (int)work.size();
+  return CCS_OK;
+}
+
 static int build_f64_lane(ccs_handle *h) {
   const Layout &L = h->L;
   const size_t nf = (size_t)L.field;
@@ -252,17 +275,9 @@ static int build_f64_lane(ccs_handle *h) {
   CCS_TRY(h, cudaMalloc(&h->d_stages, h->h_stages.size() * sizeof(F64Stage)));
   CCS_TRY(h, cudaMemcpyAsync(h->d_stages, h->h_stages.data(), h->h_stages.size() * sizeof(F64Stage),
                              cudaMemcpyHostToDevice, h->stream));
-  // work list: all tiles of the six panels
-  const int ntx = (L.N + F64_TX - 1) / F64_TX, nty = (L.N + F64_TY - 1) / F64_TY;
-  std::vector<WorkItem> work;
-  for (int p = 0; p < 6; p++)
-    for (int ty = 0; ty < nty; ty++)
-      for (int tx = 0; tx < ntx; tx++) work.push_back(WorkItem{0, (int16_t)p, (int16_t)tx, (int16_t)ty});
-  h->nwork = (int)work.size();
-  CCS_TRY(h, cudaMalloc(&h->d_work, work.size() * sizeof(WorkItem)));
-  CCS_TRY(h, cudaMemcpyAsync(h->d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
-                             h->stream));
-  h->grid = f64_max_grid(c.device, 1);
+  int rc = build_work(h, kF64Tiles[h->var], &h->d_work, &h->nwork);
+  if (rc) return rc;
+  h->grid = f64_max_grid(h->var, c.device);
   CCS_TRY(h, cudaMalloc(&h->d_partials, 2 * kDiagBlocks * sizeof(double)));
   CCS_TRY(h, cudaStreamSynchronize(h->stream));
   return CCS_OK;
@@ -273,7 +288,7 @@ static int f64_enqueue_step(ccs_handle *h, bool with_sw) {
   for (int k = 0; k < h->n_rk; k++) {
     const F64Stage *d = h->d_stages + ((k == h->n_rk - 1 && with_sw) ? h->n_rk : k);
     if (h->timing) CCS_TRY(h, cudaEventRecord(h->ev0, h->stream));
-    CCS_TRY(h, launch_f64_stage(d, h->d_work, h->nwork, h->grid, h->stream));
+    CCS_TRY(h, launch_f64_stage(h->var, d, h->d_work, h->nwork, h->grid, h->stream));
     if (h->timing) {
       CCS_TRY(h, cudaEventRecord(h->ev1, h->stream));
       CCS_TRY(h, cudaEventSynchronize(h->ev1));
@@ -548,7 +563,7 @@ int ccs_spatial_operator(ccs_handle *h, double *tp, double *tu, double *tv) {
   cudaSetDevice(h->cfg.device);
   if (h->cfg.precision == CCS_MIXED) return mixed_tend(h, tp, tu, tv);
   const F64Stage *d = h->d_stages + h->n_rk + 1;
-  CCS_TRY(h, launch_f64_stage(d, h->d_work, h->nwork, h->grid, h->stream));
+  CCS_TRY(h, launch_f64_stage(h->var, d, h->d_work, h->nwork, h->grid, h->stream));
   double *dst[3] = {tp, tu, tv};
   for (int k = 0; k < 3; k++)
     if (dst[k]) {
@@ -608,6 +623,7 @@ struct MixedLane {
   int n_rk = 0;
   WorkItem *d_work = nullptr;
   int nwork = 0, grid = 0;
+  int var = 0;  // tile variant of the mixed stage kernel (kMxTiles)
   double phibar = 0.;
   bool have_phibar = false;
   cudaGraphExec_t g_step = nullptr;
@@ -728,17 +744,9 @@ static int mixed_handle_create(ccs_handle *h) {
   for (int k = 0; k < 3; k++) { M->tend[k] = b; b += nf; }
   CCS_TRY(h, cudaMalloc(&M->staging, 8 * nref * sizeof(double)));
   CCS_TRY(h, cudaMalloc(&h->d_partials, 2 * kDiagBlocks * sizeof(double)));
-  // work list
-  const int ntx = (L.N + MX_TX - 1) / MX_TX, nty = (L.N + MX_TY - 1) / MX_TY;
-  std::vector<WorkItem> work;
-  for (int p = 0; p < 6; p++)
-    for (int ty = 0; ty < nty; ty++)
-      for (int tx = 0; tx < ntx; tx++) work.push_back(WorkItem{0, (int16_t)p, (int16_t)tx, (int16_t)ty});
-  M->nwork = (int)work.size();
-  CCS_TRY(h, cudaMalloc(&M->d_work, work.size() * sizeof(WorkItem)));
-  CCS_TRY(h, cudaMemcpyAsync(M->d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
-                             h->stream));
-  M->grid = mixed_max_grid(h->cfg.device);
+  int rc = build_work(h, kMxTiles[M->var], &M->d_work, &M->nwork);
+  if (rc) return rc;
+  M->grid = mixed_max_grid(M->var, h->cfg.device);
   CCS_TRY(h, cudaStreamSynchronize(h->stream));
   return CCS_OK;
 }
@@ -863,7 +871,7 @@ static int mixed_enqueue_step(ccs_handle *h) {
   MixedLane *M = h->mixed;
   for (int k = 0; k < M->n_rk; k++) {
     if (h->timing) CCS_TRY(h, cudaEventRecord(h->ev0, h->stream));
-    CCS_TRY(h, launch_mixed_stage(M->d_stages + k, M->d_work, M->nwork, M->grid, h->stream));
+    CCS_TRY(h, launch_mixed_stage(M->var, M->d_stages + k, M->d_work, M->nwork, M->grid, h->stream));
     if (h->timing) {
       CCS_TRY(h, cudaEventRecord(h->ev1, h->stream));
       CCS_TRY(h, cudaEventSynchronize(h->ev1));
@@ -908,7 +916,7 @@ static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv) {
   if (!M->have_phibar) return CCS_ERR_ARG;
   const Layout &L = h->L;
   const size_t nref = (size_t)L.nh * L.nh * 6;
-  CCS_TRY(h, launch_mixed_stage(M->d_stages + M->n_rk, M->d_work, M->nwork, M->grid, h->stream));
+  CCS_TRY(h, launch_mixed_stage(M->var, M->d_stages + M->n_rk, M->d_work, M->nwork, M->grid, h->stream));
   const double a2 = h->cfg.radius * h->cfg.radius;
   double *o = M->staging;
   CCS_TRY(h, launch_mixed_tend_export(L, M->tend[0], M->tend[1], M->tend[2], h->mesh->m64, a2, o, o + nref,
@@ -942,10 +950,133 @@ static int mixed_diag(ccs_handle *h, double *mass, double *energy) {
 }
 
 // ---------------------------------------------------------------------------
+// tile variants and the autotuner
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_tune_mutex;
+std::map<std::tuple<int, int, int, int>, int> g_tune_cache;  // (device, lane, N, halo) -> variant
+}  // namespace
+
+static int lane_nvar(const ccs_handle *h) { return h->cfg.precision == CCS_MIXED ? MX_NVAR : F64_NVAR; }
+
+// Switches the handle's stage kernel to tile variant var: new work list and grid;
+// the captured step graphs are dropped and re-captured on the next step.
+static int set_variant(ccs_handle *h, int var) {
+  if (var < 0 || var >= lane_nvar(h)) return CCS_ERR_ARG;
+  const int dev = h->cfg.device;
+  if (h->cfg.precision == CCS_MIXED) {
+    MixedLane *M = h->mixed;
+    if (var == M->var && M->d_work) return CCS_OK;
+    int rc = build_work(h, kMxTiles[var], &M->d_work, &M->nwork);
+    if (rc) return rc;
+    M->var = var;
+    M->grid = mixed_max_grid(var, dev);
+    if (M->g_step) {
+      cudaGraphExecDestroy(M->g_step);
+      M->g_step = nullptr;
+    }
+  } else {
+    if (var == h->var && h->d_work) return CCS_OK;
+    int rc = build_work(h, kF64Tiles[var], &h->d_work, &h->nwork);
+    if (rc) return rc;
+    h->var = var;
+    h->grid = f64_max_grid(var, dev);
+    if (h->g_step) cudaGraphExecDestroy(h->g_step);
+    if (h->g_step_sw) cudaGraphExecDestroy(h->g_step_sw);
+    h->g_step = h->g_step_sw = nullptr;
+  }
+  return CCS_OK;
+}
+
+// Mean time of one launch of the handle's first RK stage with its current variant.
+// That stage reads the state and writes only stage scratch (the next stage's input
+// and the RK accumulator), so timing it leaves the state unchanged.
+static int time_first_stage(ccs_handle *h, int reps, double *us) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CCS_TRY(h, cudaEventCreate(&e0));
+  CCS_TRY(h, cudaEventCreate(&e1));
+  auto launch = [&]() -> cudaError_t {
+    if (h->cfg.precision == CCS_MIXED) {
+      MixedLane *M = h->mixed;
+      return launch_mixed_stage(M->var, M->d_stages, M->d_work, M->nwork, M->grid, h->stream);
+    }
+    return launch_f64_stage(h->var, h->d_stages, h->d_work, h->nwork, h->grid, h->stream);
+  };
+  cudaError_t e = launch();  // warm-up
+  for (int r = 0; r < reps && e == cudaSuccess; r++) {
+    if (r == 0) e = cudaEventRecord(e0, h->stream);
+    if (e == cudaSuccess) e = launch();
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CCS_TRY(h, e);
+  *us = 1e3 * ms / reps;
+  return CCS_OK;
+}
+
+extern "C" int ccs_set_variant(ccs_handle *h, int var) {
+  if (!h) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  return set_variant(h, var);
+}
+
+extern "C" int ccs_get_variant(ccs_handle *h, int *var, int *tile_x, int *tile_y) {
+  if (!h) return CCS_ERR_ARG;
+  const bool mx = h->cfg.precision == CCS_MIXED;
+  const int v = mx ? h->mixed->var : h->var;
+  const TileShape ts = mx ? kMxTiles[v] : kF64Tiles[v];
+  if (var) *var = v;
+  if (tile_x) *tile_x = ts.tx;
+  if (tile_y) *tile_y = ts.ty;
+  return CCS_OK;
+}
+
+extern "C" int ccs_autotune(ccs_handle *h, int reps, int force, int *chosen, double *times_us) {
+  if (!h || reps < 1) return CCS_ERR_ARG;
+  if (h->cfg.precision == CCS_MIXED && !h->mixed->have_phibar) return CCS_ERR_ARG;  // state not set
+  cudaSetDevice(h->cfg.device);
+  const int nvar = lane_nvar(h);
+  if (times_us)
+    for (int v = 0; v < CCS_MAX_VARIANTS; v++) times_us[v] = 0.;
+  const auto key = std::make_tuple(h->cfg.device, h->cfg.precision, h->L.N, h->L.h);
+  int best = -1;
+  if (!force) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) best = it->second;
+  }
+  if (best < 0) {
+    double best_us = 0.;
+    for (int v = 0; v < nvar; v++) {
+      int rc = set_variant(h, v);
+      if (rc) return rc;
+      double us = 0.;
+      rc = time_first_stage(h, reps, &us);
+      if (rc) return rc;
+      if (times_us) times_us[v] = us;
+      if (best < 0 || us < best_us) {
+        best = v;
+        best_us = us;
+      }
+    }
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = best;
+  }
+  int rc = set_variant(h, best);
+  if (rc) return rc;
+  if (chosen) *chosen = best;
+  return CCS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // batches: one launch per lane and RK stage over the union of the members' tiles
 // ---------------------------------------------------------------------------
 struct BatchGroup {
-  int lane = 0, n_rk = 0, nmem = 0;
+  int lane = 0, n_rk = 0, nmem = 0, var = 0;
   std::vector<ccs_handle *> members;
   void *d_stages = nullptr;  // [n_rk + 1][nmem] F64Stage or MixedStage (last row: F64 final with sphere winds)
   WorkItem *d_work = nullptr;
@@ -975,11 +1106,11 @@ static int batch_enqueue(ccs_batch *b, bool with_sw) {
       cudaError_t e;
       if (g.lane == CCS_FP64) {
         const int row = (k == g.n_rk - 1 && with_sw) ? g.n_rk : k;
-        e = launch_f64_stage((const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork, g.grid,
-                             g.stream);
+        e = launch_f64_stage(g.var, (const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork,
+                             g.grid, g.stream);
       } else {
-        e = launch_mixed_stage((const MixedStage *)g.d_stages + (size_t)k * g.nmem, g.d_work, g.nwork, g.grid,
-                               g.stream);
+        e = launch_mixed_stage(g.var, (const MixedStage *)g.d_stages + (size_t)k * g.nmem, g.d_work, g.nwork,
+                               g.grid, g.stream);
       }
       if (e != cudaSuccess) {
         b->err = cudaGetErrorString(e);
@@ -1007,19 +1138,24 @@ extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **o
   b->members.assign(members, members + n);
   cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  auto member_var = [](const ccs_handle *m) { return m->cfg.precision == CCS_MIXED ? m->mixed->var : m->var; };
   for (int lane = 0; lane < 2; lane++)
-    for (int scheme = 0; scheme < 2; scheme++) {
+    for (int scheme = 0; scheme < 2; scheme++)
+      for (int var = 0; var < (lane == CCS_FP64 ? F64_NVAR : MX_NVAR); var++) {
       BatchGroup g;
       g.lane = lane;
+      g.var = var;
       for (int k = 0; k < n; k++)
-        if (members[k]->cfg.precision == lane && members[k]->cfg.scheme == scheme) g.members.push_back(members[k]);
+        if (members[k]->cfg.precision == lane && members[k]->cfg.scheme == scheme && member_var(members[k]) == var)
+          g.members.push_back(members[k]);
       if (g.members.empty()) continue;
       g.nmem = (int)g.members.size();
       g.n_rk = scheme == CCS_RK4 ? 4 : 3;
       cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
       cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
       std::vector<WorkItem> work;
-      const int TXg = lane == CCS_FP64 ? F64_TX : MX_TX, TYg = lane == CCS_FP64 ? F64_TY : MX_TY;
+      const TileShape ts = lane == CCS_FP64 ? kF64Tiles[var] : kMxTiles[var];
+      const int TXg = ts.tx, TYg = ts.ty;
       for (int m = 0; m < g.nmem; m++) {
         const int N = g.members[m]->cfg.N;
         const int ntx = (N + TXg - 1) / TXg, nty = (N + TYg - 1) / TYg;
@@ -1037,14 +1173,14 @@ extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **o
           for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->h_stages[k];
         cudaMalloc(&g.d_stages, st.size() * sizeof(F64Stage));
         cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(F64Stage), cudaMemcpyHostToDevice);
-        g.grid = f64_max_grid(dev, 1);
+        g.grid = f64_max_grid(var, dev);
       } else {
         std::vector<MixedStage> st((size_t)g.n_rk * g.nmem);
         for (int k = 0; k < g.n_rk; k++)
           for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->mixed->h_stages[k];
         cudaMalloc(&g.d_stages, st.size() * sizeof(MixedStage));
         cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(MixedStage), cudaMemcpyHostToDevice);
-        g.grid = mixed_max_grid(dev);
+        g.grid = mixed_max_grid(var, dev);
       }
       b->groups.push_back(g);
     }

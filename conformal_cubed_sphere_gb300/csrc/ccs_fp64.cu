@@ -23,11 +23,15 @@ namespace ccs {
 
 namespace {
 
-constexpr int TX = F64_TX, TY = F64_TY, NT = F64_THREADS;
-constexpr int RX = TX + 6, RY = TY + 6, RN = RX * RY;
-constexpr int NFX = TY * (TX + 1), NFY = (TY + 1) * TX, NF = NFX + NFY;
+// a tile of TX x TY cells; phase 3 maps one thread to one cell
+template <int TX_, int TY_>
+struct F64Tile {
+  static constexpr int TX = TX_, TY = TY_, NT = TX * TY;
+  static constexpr int RX = TX + 6, RY = TY + 6, RN = RX * RY;
+  static constexpr int NFX = TY * (TX + 1), NFY = (TY + 1) * TX, NF = NFX + NFY;
+};
+constexpr int NT = 256;
 constexpr int NCELL_ARR = 11;
-static_assert(TX * TY == NT, "phase 3 maps one thread to one cell");
 
 }  // namespace
 
@@ -107,6 +111,7 @@ __device__ __forceinline__ double central_diff(int op, const double *f, int s, d
   return (-f[-3 * s] + 9. * f[-2 * s] - 45. * f[-s] + 45. * f[s] - 9. * f[2 * s] + f[3 * s]) / (60. * d);
 }
 
+template <int RN>
 struct Smem {
   // cell quantities on the halo'd tile (row-major [RY][RX])
   double phit[RN], phitG[RN], E[RN], Fx[RN], Fy[RN], uC[RN], vC[RN], ig11[RN], ig22[RN], u[RN], v[RN];
@@ -116,10 +121,13 @@ __device__ __forceinline__ bool is_corner(int i, int j, int N) {
   return (i < 1 || i > N) && (j < 1 || j > N);
 }
 
+template <class T>
 __global__ void __launch_bounds__(NT, 2)
 f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
+  constexpr int TX = T::TX, TY = T::TY, RX = T::RX, RN = T::RN, NFX = T::NFX, NF = T::NF;
+  static_assert(T::NT == NT, "phase 3 maps one thread to one cell");
   extern __shared__ __align__(16) double smem_raw[];
-  Smem &S = *reinterpret_cast<Smem *>(smem_raw);
+  Smem<RN> &S = *reinterpret_cast<Smem<RN> *>(smem_raw);
   double *rec = smem_raw + NCELL_ARR * RN;  // [nrec][NF]
   const int tid = threadIdx.x;
 
@@ -376,33 +384,63 @@ cudaError_t launch_div_const_check(const double *x, int64_t n, double b, double 
   return cudaGetLastError();
 }
 
-int f64_stage_smem_bytes(int ediss) {
-  return (int)((NCELL_ARR * RN + (ediss ? 8 : 6) * NF) * sizeof(double));
+namespace {
+
+using F64T0 = F64Tile<32, 8>;
+using F64T1 = F64Tile<16, 16>;
+using F64T2 = F64Tile<64, 4>;
+
+template <class T>
+constexpr int f64_smem_bytes() {  // sized for the E-reconstruction variant (8 face arrays)
+  return (int)((NCELL_ARR * T::RN + 8 * T::NF) * sizeof(double));
 }
 
-int f64_max_grid(int device, int ediss) {
+template <class T>
+int f64_grid_for(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  const int smem = f64_stage_smem_bytes(ediss);
-  cudaFuncSetAttribute(f64_stage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f64_stage_kernel, NT, smem);
+  constexpr int smem = f64_smem_bytes<T>();
+  cudaFuncSetAttribute(f64_stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f64_stage_kernel<T>, NT, smem);
   if (per < 1) per = 1;
   return sms * per;
 }
 
-cudaError_t launch_f64_stage(const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid,
-                             cudaStream_t s) {
-  // all stages of a launch share one ediss setting; size for the larger variant
-  const int smem = f64_stage_smem_bytes(1);
+template <class T>
+cudaError_t f64_launch(const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
+  constexpr int smem = f64_smem_bytes<T>();
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(f64_stage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(f64_stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr_set = true;
   }
   if (grid > nwork) grid = nwork;
   if (grid < 1) return cudaSuccess;
-  f64_stage_kernel<<<grid, NT, smem, s>>>(d_stages, d_work, nwork);
+  f64_stage_kernel<T><<<grid, NT, smem, s>>>(d_stages, d_work, nwork);
   return cudaGetLastError();
+}
+
+static_assert(F64T0::TX == kF64Tiles[0].tx && F64T0::TY == kF64Tiles[0].ty, "tile table");
+static_assert(F64T1::TX == kF64Tiles[1].tx && F64T1::TY == kF64Tiles[1].ty, "tile table");
+static_assert(F64T2::TX == kF64Tiles[2].tx && F64T2::TY == kF64Tiles[2].ty, "tile table");
+
+}  // namespace
+
+int f64_max_grid(int var, int device) {
+  switch (var) {
+    case 1: return f64_grid_for<F64T1>(device);
+    case 2: return f64_grid_for<F64T2>(device);
+    default: return f64_grid_for<F64T0>(device);
+  }
+}
+
+cudaError_t launch_f64_stage(int var, const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid,
+                             cudaStream_t s) {
+  switch (var) {
+    case 1: return f64_launch<F64T1>(d_stages, d_work, nwork, grid, s);
+    case 2: return f64_launch<F64T2>(d_stages, d_work, nwork, grid, s);
+    default: return f64_launch<F64T0>(d_stages, d_work, nwork, grid, s);
+  }
 }
 
 // ---- diagnostics: calc_total_mass / calc_total_energy (diag_mod.F90:10-53) ------

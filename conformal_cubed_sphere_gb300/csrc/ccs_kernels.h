@@ -59,16 +59,24 @@ struct MixedStage {
   int kind, ediss;
 };
 
-// kernel launchers (return cudaGetLastError())
-cudaError_t launch_f64_stage(const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid,
-                             cudaStream_t s);
-int f64_stage_smem_bytes(int ediss);
-int f64_max_grid(int device, int ediss);
+// Kernel variants: the tile shape (cells per work item) of each lane's stage kernel.
+// A handle runs one variant; the autotuner picks it per resolution by timing.
+struct TileShape {
+  int tx, ty;
+};
+constexpr int F64_NVAR = 3;  // 32 x 8, 16 x 16, 64 x 4 (256 threads, one cell each in phase 3)
+constexpr TileShape kF64Tiles[F64_NVAR] = {{32, 8}, {16, 16}, {64, 4}};
+constexpr int MX_NVAR = 2;  // 32 x 32 (256 threads), 32 x 16 (128 threads)
+constexpr TileShape kMxTiles[MX_NVAR] = {{32, 32}, {32, 16}};
 
-cudaError_t launch_mixed_stage(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid,
+// kernel launchers (return cudaGetLastError()); `var` indexes the tile tables
+cudaError_t launch_f64_stage(int var, const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid,
+                             cudaStream_t s);
+int f64_max_grid(int var, int device);
+
+cudaError_t launch_mixed_stage(int var, const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid,
                                cudaStream_t s);
-int mixed_max_grid(int device);
-int mixed_smem_bytes();
+int mixed_max_grid(int var, int device);
 cudaError_t launch_mixed_import(const Layout &L, const double *phi, const double *u, const double *v,
                                 double phibar, double inv_a2, StateMixed out, float *lohp, float *lou,
                                 float *lov, cudaStream_t s);
@@ -82,9 +90,6 @@ cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp,
                               const float *lov, const MeshF64 &m, double phibar, double a2, double *partials,
                               int nblocks, cudaStream_t s);
 
-// tile shapes
-constexpr int F64_TX = 32, F64_TY = 8, F64_THREADS = 256;
-constexpr int MX_TX = 32, MX_TY = 32, MX_THREADS = 256;
 
 // test support: correctly rounded division by a constant, see ccs_fp64.cu
 cudaError_t launch_div_const_check(const double *x, int64_t n, double b, double *out, cudaStream_t s);

@@ -21,12 +21,19 @@ namespace ccs {
 
 namespace {
 
-constexpr int TX = MX_TX, TY = MX_TY, NT = MX_THREADS;
-constexpr int RX = TX + 6, RY = TY + 6;  // halo'd tile
-constexpr int SP = RX + 1;               // odd pitch: a warp reading one column hits 32 banks
-constexpr int RN = RY * SP;
-constexpr int NFL = TX + 1;              // faces per tile line
-static_assert(TX == 32 && TY == 32 && NT == 256, "lanes map to the 32 rows / columns of a tile");
+// A tile of 32 x TY cells (TY = 32 or 16) and 8 TY threads.  Phase 2 gives each of
+// the TY rows four threads (segments of its 33 x-faces) and each of the 32 columns
+// TY / 8 threads (segments of its TY + 1 y-faces); phase 3 gives each thread four cells.
+template <int TY_>
+struct MxTile {
+  static constexpr int TX = 32, TY = TY_, NT = 8 * TY;
+  static constexpr int RX = TX + 6, RY = TY + 6;  // halo'd tile
+  static constexpr int SP = RX + 1;               // odd pitch: a warp reading one column hits 32 banks
+  static constexpr int RN = RY * SP;
+  static constexpr int NFL = TX + 1;              // x-faces per tile row
+  static_assert(TY % 8 == 0 && TY <= 32, "column segments of eight faces");
+};
+constexpr int SP = 39;  // the smem row pitch, the same for every tile height
 
 // Difference-form WENO-Z (spatial_operators_mod.F90:282-361) of one cell for both
 // directions.  d0..d3 = Q(c-1)-Q(c-2), Q(c)-Q(c-1), Q(c+1)-Q(c), Q(c+2)-Q(c+1).
@@ -76,12 +83,79 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
   }
 }
 
+// weno_d for two fields at once (the mass flux and phitG of one line): the same
+// operations, lane for lane, on float2 pairs, so that the FP32 adds, multiplies and
+// FMAs issue as paired f32x2 instructions; divisions, comparisons and selections
+// stay per lane.  Bit for bit the two scalar calls.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {  // RN(a - b): b (-1) is exact
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 k2(float c) { return make_float2(c, c); }
+
+__device__ __forceinline__ void weno_d2(float2 d0, float2 d1, float2 d2, float2 d3, float2 eps, float2 &Dp,
+                                        float2 &Dm) {
+  const float2 A1 = sub2(d1, d0), A2 = sub2(d2, d1), A3 = sub2(d3, d2);
+  const float2 B1 = __ffma2_rn(k2(3.f), d1, sub2(k2(0.f), d0));
+  const float2 B2 = __fadd2_rn(d1, d2), B3 = __ffma2_rn(k2(-3.f), d2, d3);
+  const float k133 = 13.f / 3.f;
+  const float2 b1 = __ffma2_rn(__fmul2_rn(k2(k133), A1), A1, __fmul2_rn(B1, B1));
+  const float2 b2 = __ffma2_rn(__fmul2_rn(k2(k133), A2), A2, __fmul2_rn(B2, B2));
+  const float2 b3 = __ffma2_rn(__fmul2_rn(k2(k133), A3), A3, __fmul2_rn(B3, B3));
+  const float2 D12 = sub2(b1, b2), D23 = sub2(b2, b3), D31 = sub2(b3, b1);
+  const float2 e1 = __fadd2_rn(eps, b1), e2 = __fadd2_rn(eps, b2), e3 = __fadd2_rn(eps, b3);
+  const float2 p1 = __ffma2_rn(k2(5.f / 6.f), d1, __fmul2_rn(k2(-(1.f / 3.f)), d0));
+  const float2 p2 = __ffma2_rn(k2(1.f / 6.f), d1, __fmul2_rn(k2(1.f / 3.f), d2));
+  const float2 p3 = __ffma2_rn(k2(2.f / 3.f), d2, __fmul2_rn(k2(-(1.f / 6.f)), d3));
+  const float2 m1 = __ffma2_rn(k2(-5.f / 6.f), d2, __fmul2_rn(k2(1.f / 3.f), d3));
+  const float2 m2 = __ffma2_rn(k2(-1.f / 6.f), d2, __fmul2_rn(k2(-(1.f / 3.f)), d1));
+  const float2 m3 = __ffma2_rn(k2(-2.f / 3.f), d1, __fmul2_rn(k2(1.f / 6.f), d0));
+  const float2 sa = __ffma2_rn(k2(1.f / 3.f), p1, __fmul2_rn(k2(2.f / 3.f), p2));
+  const float2 sb = __ffma2_rn(k2(2.f / 3.f), p2, __fmul2_rn(k2(1.f / 3.f), p3));
+  const float2 ta = __ffma2_rn(k2(1.f / 3.f), m1, __fmul2_rn(k2(2.f / 3.f), m2));
+  const float2 tb = __ffma2_rn(k2(2.f / 3.f), m2, __fmul2_rn(k2(1.f / 3.f), m3));
+  float2 r1, r2, r3;
+  bool lo40[2], lo41[2], hi40[2], hi41[2], lt40[2], lt41[2];
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const float t40 = fabsf(q ? D12.y : D12.x), t41 = fabsf(q ? D23.y : D23.x), t5 = fabsf(q ? D31.y : D31.x);
+    const float mn = fminf(q ? b1.y : b1.x, fminf(q ? b2.y : b2.x, q ? b3.y : b3.x));
+    const float x1 = __fdividef(t5, q ? e1.y : e1.x), x2 = __fdividef(t5, q ? e2.y : e2.x),
+                x3 = __fdividef(t5, q ? e3.y : e3.x);
+    if (q) { r1.y = x1; r2.y = x2; r3.y = x3; } else { r1.x = x1; r2.x = x2; r3.x = x3; }
+    lo40[q] = t40 <= mn; lo41[q] = t41 <= mn; hi40[q] = t40 > mn; hi41[q] = t41 > mn;
+    lt40[q] = t40 < mn; lt41[q] = t41 < mn;
+  }
+  {  // "+" weights
+    const float2 a1 = __ffma2_rn(k2(0.1f), r1, k2(0.1f)), a2 = __ffma2_rn(k2(0.6f), r2, k2(0.6f)),
+                 a3 = __ffma2_rn(k2(0.3f), r3, k2(0.3f));
+    const float2 num = __ffma2_rn(a1, p1, __ffma2_rn(a2, p2, __fmul2_rn(a3, p3)));
+    const float2 den = __fadd2_rn(__fadd2_rn(a1, a2), a3);
+    float vx = __fdividef(num.x, den.x), vy = __fdividef(num.y, den.y);
+    vx = (hi40[0] && lt41[0]) ? sb.x : vx;
+    vy = (hi40[1] && lt41[1]) ? sb.y : vy;
+    Dp.x = (lo40[0] && hi41[0]) ? sa.x : vx;
+    Dp.y = (lo40[1] && hi41[1]) ? sa.y : vy;
+  }
+  {  // "-" weights
+    const float2 a1 = __ffma2_rn(k2(0.1f), r3, k2(0.1f)), a2 = __ffma2_rn(k2(0.6f), r2, k2(0.6f)),
+                 a3 = __ffma2_rn(k2(0.3f), r1, k2(0.3f));
+    const float2 num = __ffma2_rn(a1, m1, __ffma2_rn(a2, m2, __fmul2_rn(a3, m3)));
+    const float2 den = __fadd2_rn(__fadd2_rn(a1, a2), a3);
+    float vx = __fdividef(num.x, den.x), vy = __fdividef(num.y, den.y);
+    vx = (hi41[0] && lt40[0]) ? tb.x : vx;
+    vy = (hi41[1] && lt40[1]) ? tb.y : vy;
+    Dm.x = (lo41[0] && hi40[0]) ? ta.x : vx;
+    Dm.y = (lo41[1] && hi40[1]) ? ta.y : vy;
+  }
+}
+
+template <class T>
 struct SmemMx {
   MixedStage st;  // this work item's stage descriptor
   // cell quantities on the halo'd tile, [row][col] with pitch SP
-  float F[RN], G[RN], E[RN], hs[RN], s[RN], uC[RN], vC[RN], u[RN], v[RN];
-  float gx[2][TY][NFL];  // x-face (flux, E) values minus the value of the cell left of the face
-  float gy[2][NFL][TX];  // y-face values minus the value of the cell below the face
+  float F[T::RN], G[T::RN], E[T::RN], hs[T::RN], s[T::RN], uC[T::RN], vC[T::RN], u[T::RN], v[T::RN];
+  float gx[2][T::TY][T::NFL];     // x-face (flux, E) values minus the value of the cell left of the face
+  float gy[2][T::TY + 1][T::TX];  // y-face values minus the value of the cell below the face
 };
 
 __device__ __forceinline__ bool corner(int i, int j, int N) { return (i < 1 || i > N) && (j < 1 || j > N); }
@@ -90,14 +164,15 @@ __device__ __forceinline__ bool corner(int i, int j, int N) { return (i < 1 || i
 // the cells' difference windows slide along the line so that each cell costs one
 // new shared-memory value per field; the face between two cells is formed from
 // the left cell's "+" and the right cell's "-" corrections in registers.
-template <bool XDIR>
-__device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Qflux, const float *__restrict__ cvel,
-                                          const float *__restrict__ lam, const Layout &L, int lane, int f0,
+template <bool XDIR, class T>
+__device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict__ Qflux,
+                                          const float *__restrict__ cvel, const float *__restrict__ lam,
+                                          const Layout &L, int line, int f0,
                                           int NFACE, int startg, int lineg) {
   const MixedStage &st = S.st;
   const float phibar = st.phibar, epsF = 4.f * st.eps_F, epsE = 4.f * st.eps_E, epsP = 4.f * st.eps_P;
   const int stp = XDIR ? 1 : SP;
-  const int base = XDIR ? (lane + 3) * SP + 2 : 2 * SP + lane + 3;  // cell ci = 0 of the line
+  const int base = XDIR ? (line + 3) * SP + 2 : 2 * SP + line + 3;  // cell ci = 0 of the line
   int o = base + (f0 - 2) * stp;
   // window values at cells c-2 .. c+1 for c = f0
   float Fv[4], Ev[4], hv[4], sv[4];
@@ -134,9 +209,18 @@ __device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Q
     const float qn = hn * sn;
     const float dF3 = Fn - Flast, dE3 = En - Elast, dP3 = fmaf(phibar, sn - slast, qn - qlast);
     float DFp, DFm, DEp, DEm, DPp, DPm;
+#ifdef CCS_MIXED_SCALAR_WENO
     weno_d(dF0, dF1, dF2, dF3, epsF, DFp, DFm);
-    weno_d(dE0, dE1, dE2, dE3, epsE, DEp, DEm);
     weno_d(dP0, dP1, dP2, dP3, epsP, DPp, DPm);
+#else
+    {
+      float2 Dp2, Dm2;
+      weno_d2(make_float2(dF0, dP0), make_float2(dF1, dP1), make_float2(dF2, dP2), make_float2(dF3, dP3),
+              make_float2(epsF, epsP), Dp2, Dm2);
+      DFp = Dp2.x; DPp = Dp2.y; DFm = Dm2.x; DPm = Dm2.y;
+    }
+#endif
+    weno_d(dE0, dE1, dE2, dE3, epsE, DEp, DEm);
     const float uc = cvel[base + ci * stp];
     if (k > 0) {
       const int fi = ci - 1;         // face between line cells ci-1 and ci
@@ -148,11 +232,11 @@ __device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Q
         const float gF = 0.5f * (dF1 + pDFp + DFm - lm * (dP1 + DPm - pDPp));
         const float gE = 0.5f * (dE1 + pDEp + DEm);
         if (XDIR) {
-          S.gx[0][lane][fi] = gF;
-          S.gx[1][lane][fi] = gE;
+          S.gx[0][line][fi] = gF;
+          S.gx[1][line][fi] = gE;
         } else {
-          S.gy[0][fi][lane] = gF;
-          S.gy[1][fi][lane] = gE;
+          S.gy[0][fi][line] = gF;
+          S.gy[1][fi][line] = gE;
         }
       }
     }
@@ -170,10 +254,13 @@ __device__ __forceinline__ void tile_line(SmemMx &S, const float *__restrict__ Q
 #define CCS_MIXED_MIN_CTAS 3
 #endif
 
-__global__ void __launch_bounds__(NT, CCS_MIXED_MIN_CTAS)
+template <class T>
+__global__ void __launch_bounds__(T::NT, CCS_MIXED_MIN_CTAS * 32 / T::TY)
 mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
+  constexpr int TX = T::TX, TY = T::TY, NT = T::NT, RX = T::RX, RY = T::RY;
+  static_assert(T::SP == SP, "smem pitch");
   extern __shared__ __align__(16) float smem_f[];
-  SmemMx &S = *reinterpret_cast<SmemMx *>(smem_f);
+  SmemMx<T> &S = *reinterpret_cast<SmemMx<T> *>(smem_f);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -224,13 +311,15 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
 
     // ---- phase 2: lines -> face values (warps 0-3 rows, 4-7 columns) ---------
     {
-      const int seg = warp & 3;
-      const int f0 = seg == 0 ? 0 : 1 + 8 * seg;  // faces 0-8, 9-16, 17-24, 25-32
-      const int nface = seg == 0 ? 9 : 8;
-      if (warp < 4) {
-        if (j0 + lane <= N) tile_line<true>(S, S.F, S.uC, st.m.lamx, L, lane, f0, nface, i0 - 1, j0 + lane);
+      // segment seg of a line covers faces 0-8 (seg 0) or 8 seg + 1 .. 8 seg + 8
+      if (tid < 4 * TY) {
+        const int line = tid % TY, seg = tid / TY;
+        const int f0 = seg == 0 ? 0 : 1 + 8 * seg, nface = seg == 0 ? 9 : 8;
+        if (j0 + line <= N) tile_line<true>(S, S.F, S.uC, st.m.lamx, L, line, f0, nface, i0 - 1, j0 + line);
       } else {
-        if (i0 + lane <= N) tile_line<false>(S, S.G, S.vC, st.m.lamy, L, lane, f0, nface, j0 - 1, i0 + lane);
+        const int t = tid - 4 * TY, line = t % TX, seg = t / TX;
+        const int f0 = seg == 0 ? 0 : 1 + 8 * seg, nface = seg == 0 ? 9 : 8;
+        if (i0 + line <= N) tile_line<false>(S, S.G, S.vC, st.m.lamy, L, line, f0, nface, j0 - 1, i0 + line);
       }
     }
     __syncthreads();
@@ -238,7 +327,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     // ---- phase 3: tendencies, stage update, ghost push -------------------------
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int li = lane, lj = warp + 8 * k;
+      const int li = lane, lj = warp + (NT / 32) * k;
       const int i = i0 + li, j = j0 + lj;
       if (i > N || j > N) continue;
       const int r = (lj + 3) * SP + li + 3;
@@ -330,34 +419,31 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     if (st.kind != K_TEND) {
       const int h = L.h;
       // strips: 0 left (k = i), 1 right (k = N+1-i), 2 below (k = j), 3 above (k = N+1-j);
-      // each tile pushes the strip cells it owns: cross-edge range [xlo, xhi]
-      // (i for left/right, j for below/above) and along-edge range [alo, ahi]
+      // each tile pushes the strip cells it owns, strip by strip: entries [o_sd, o_sd+1)
+      // cover the cross-edge cells x (i for left/right, j for below/above) times the
+      // tile's cells m along the edge
       const int ie = min(i0 + TX - 1, N), je = min(j0 + TY - 1, N);
-      int xlo[4], xhi[4], alo[4], ahi[4], off[5];
-      xlo[0] = i0; xhi[0] = min(ie, h); alo[0] = j0; ahi[0] = je;
-      xlo[1] = max(i0, N - h + 1); xhi[1] = ie; alo[1] = j0; ahi[1] = je;
-      xlo[2] = j0; xhi[2] = min(je, h); alo[2] = i0; ahi[2] = ie;
-      xlo[3] = max(j0, N - h + 1); xhi[3] = je; alo[3] = i0; ahi[3] = ie;
-      off[0] = 0;
-      for (int sd = 0; sd < 4; sd++) {
-        const int nx = xhi[sd] - xlo[sd] + 1, na = ahi[sd] - alo[sd] + 1;
-        off[sd + 1] = off[sd] + (nx > 0 && na > 0 ? nx * na : 0);
-      }
-      for (int t = tid; t < off[4]; t += NT) {
-        int sd = 0;
-        while (t >= off[sd + 1]) sd++;
-        const int q = t - off[sd];
-        const int na = ahi[sd] - alo[sd] + 1;
-        const int x = xlo[sd] + q / na, m = alo[sd] + q % na;
+      const int xlo1 = max(i0, N - h + 1), xlo3 = max(j0, N - h + 1);
+      const int na01 = je - j0 + 1, na23 = ie - i0 + 1;  // along-edge lengths
+      const int o1 = max(min(ie, h) - i0 + 1, 0) * na01;
+      const int o2 = o1 + max(ie - xlo1 + 1, 0) * na01;
+      const int o3 = o2 + max(min(je, h) - j0 + 1, 0) * na23;
+      const int o4 = o3 + max(je - xlo3 + 1, 0) * na23;
+      for (int t = tid; t < o4; t += NT) {
+        const int sd = (t >= o1) + (t >= o2) + (t >= o3);
+        const int q = t - (sd == 0 ? 0 : sd == 1 ? o1 : sd == 2 ? o2 : o3);
+        const int na = sd < 2 ? na01 : na23;
+        const int xl = sd == 0 ? i0 : sd == 1 ? xlo1 : sd == 2 ? j0 : xlo3;
+        const int x = xl + q / na, m = (sd < 2 ? j0 : i0) + q % na;
         const int k = (sd == 0 || sd == 2) ? x : N + 1 - x;
         const int i = sd < 2 ? x : m, j = sd < 2 ? m : x;
         const int64_t c = L.idx(i, j, p);
         const int64_t e = ((int64_t)p * 4 + sd) * h * N + (int64_t)(k - 1) * N + (m - 1);
         const int64_t d = st.m.push[e];
-        const double *T = st.m.xf + 4 * e;
+        const double *X = st.m.xf + 4 * e;
         const float np = st.out.hp[c], nu = st.out.u[c], nv = st.out.v[c];
-        const double ud = T[0] * (double)nu + T[1] * (double)nv;
-        const double vd = T[2] * (double)nu + T[3] * (double)nv;
+        const double ud = X[0] * (double)nu + X[1] * (double)nv;
+        const double vd = X[2] * (double)nu + X[3] * (double)nv;
         st.out.hp[d] = np;
         st.out.u[d] = (float)ud;
         st.out.v[d] = (float)vd;
@@ -480,23 +566,48 @@ __global__ void mixed_diag_kernel(Layout L, StateMixed st, const float *__restri
 
 }  // namespace
 
-int mixed_smem_bytes() { return (int)sizeof(SmemMx); }
+namespace {
 
-int mixed_max_grid(int device) {
+using MxT0 = MxTile<32>;
+using MxT1 = MxTile<16>;
+static_assert(MxT0::TX == kMxTiles[0].tx && MxT0::TY == kMxTiles[0].ty, "tile table");
+static_assert(MxT1::TX == kMxTiles[1].tx && MxT1::TY == kMxTiles[1].ty, "tile table");
+
+template <class T>
+int mx_grid_for(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaFuncSetAttribute(mixed_stage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mixed_smem_bytes());
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel, NT, mixed_smem_bytes());
+  constexpr int smem = (int)sizeof(SmemMx<T>);
+  cudaFuncSetAttribute(mixed_stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel<T>, T::NT, smem);
   if (per < 1) per = 1;
   return sms * per;
 }
 
-cudaError_t launch_mixed_stage(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid,
-                               cudaStream_t s) {
+template <class T>
+cudaError_t mx_launch(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
+  constexpr int smem = (int)sizeof(SmemMx<T>);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(mixed_stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr_set = true;
+  }
   if (grid > nwork) grid = nwork;
   if (grid < 1) return cudaSuccess;
-  mixed_stage_kernel<<<grid, NT, mixed_smem_bytes(), s>>>(d_stages, d_work, nwork);
+  mixed_stage_kernel<T><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
   return cudaGetLastError();
+}
+
+}  // namespace
+
+int mixed_max_grid(int var, int device) {
+  return var == 1 ? mx_grid_for<MxT1>(device) : mx_grid_for<MxT0>(device);
+}
+
+cudaError_t launch_mixed_stage(int var, const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid,
+                               cudaStream_t s) {
+  return var == 1 ? mx_launch<MxT1>(d_stages, d_work, nwork, grid, s)
+                  : mx_launch<MxT0>(d_stages, d_work, nwork, grid, s);
 }
 
 static int ew_grid(const Layout &L) {

@@ -219,6 +219,25 @@ class Stepper:
         """The spatial operator (CCS_OP_WENO or CCS_OP_CENTRAL2/4/6), FP64 lane."""
         L.check(L.lib().ccs_set_operator(self.handle, int(op)), "ccs_set_operator", self.handle)
 
+    def autotune(self, reps: int = 5, force: bool = False):
+        """Picks the fastest tile variant of this lane for this grid (ccs_autotune);
+        returns (variant, per-variant mean launch times in us, 0 where not timed)."""
+        v = C.c_int()
+        t = (C.c_double * L.CCS_MAX_VARIANTS)()
+        L.check(L.lib().ccs_autotune(self.handle, int(reps), int(bool(force)), C.byref(v), t), "ccs_autotune",
+                self.handle)
+        return v.value, list(t)
+
+    def set_variant(self, var: int):
+        L.check(L.lib().ccs_set_variant(self.handle, int(var)), "ccs_set_variant", self.handle)
+
+    @property
+    def variant(self):
+        """(variant, tile_x, tile_y) of this handle's stage kernel."""
+        v, tx, ty = C.c_int(), C.c_int(), C.c_int()
+        L.check(L.lib().ccs_get_variant(self.handle, C.byref(v), C.byref(tx), C.byref(ty)), "ccs_get_variant")
+        return v.value, tx.value, ty.value
+
     def close(self):
         if self.handle:
             L.lib().ccs_destroy(self.handle)

@@ -157,6 +157,23 @@ int ccs_sync(ccs_handle *h);
  * it is created.  No counterpart call in the reference. */
 int ccs_set_operator(ccs_handle *h, int op);
 
+/* ---- kernel variants and the autotuner (no counterpart in the reference) ----
+ * Each lane's stage kernel comes in tile-shape variants (cells per work item):
+ * FP64 lane 0: 32x8, 1: 16x16, 2: 64x4; mixed lane 0: 32x32, 1: 32x16.  Every
+ * variant computes the same per-cell arithmetic, so results do not depend on the
+ * choice.  ccs_autotune times the handle's first RK stage (which writes only stage
+ * scratch, so the state is unchanged) `reps` times with each variant after one
+ * warm-up launch and keeps the fastest; the choice is cached per (device, lane, N,
+ * halo) for the process, and later calls with force = 0 reuse it without timing.
+ * The state must be set first.  chosen (may be NULL) receives the variant,
+ * times_us (may be NULL, CCS_MAX_VARIANTS entries) the mean launch times in
+ * microseconds (0 where nothing was timed).  A batch groups its members by
+ * variant, so tune members before ccs_batch_create. */
+#define CCS_MAX_VARIANTS 4
+int ccs_autotune(ccs_handle *h, int reps, int force, int *chosen, double *times_us);
+int ccs_set_variant(ccs_handle *h, int variant);
+int ccs_get_variant(ccs_handle *h, int *variant, int *tile_x, int *tile_y);
+
 /* spatial_operator(stat(old), tend) (spatial_operators_mod.F90:13-181): the
  * tendencies of phiG, u, v of the current state, interior cells (halo and corner
  * entries of the outputs are set to 0).  Any output pointer may be NULL. */

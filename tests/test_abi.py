@@ -108,3 +108,10 @@ def test_streamfunction_winds_are_nondivergent():
 
 def test_set_operator_rejects_null_handle_without_device():
     assert L.lib().ccs_set_operator(None, L.CCS_OP_CENTRAL4) == L.CCS_ERR_ARG
+
+
+def test_autotune_entry_points_reject_null_handle_without_device():
+    lib = L.lib()
+    assert lib.ccs_autotune(None, 3, 0, None, None) == L.CCS_ERR_ARG
+    assert lib.ccs_set_variant(None, 0) == L.CCS_ERR_ARG
+    assert lib.ccs_get_variant(None, None, None, None) == L.CCS_ERR_ARG

@@ -1,0 +1,101 @@
+"""Tile variants of the stage kernels and the autotuner: every variant gives the
+same bits (FP64 lane: the oracle's), the autotuner leaves the state unchanged and
+caches its choice, and batches group members by variant."""
+import numpy as np
+import pytest
+
+from conformal_cubed_sphere_gb300 import _lib as L
+from conformal_cubed_sphere_gb300 import model as M
+from oracle import oracle as O
+from tests.helpers import CHECK_FIELDS, bitwise_equal, max_rel, seeded_case, valid_mask
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("var", [0, 1, 2])
+@pytest.mark.parametrize("N", [20, 33])
+def test_fp64_variants_bitwise_against_oracle(var, N):
+    mesh, s, dt = seeded_case(N, 3, seed=4, oro=True)
+    g = M.Stepper(mesh, dt, precision="fp64")
+    g.set_variant(var)
+    assert g.variant[0] == var
+    g.set_state(s)
+    g.step(2)
+    orc = O.Oracle.from_mesh(mesh)
+    orc.set_state(s.arrays)
+    orc.run(dt, 2)
+    a, b = g.get_state(), orc.get_state()
+    m = valid_mask(mesh)
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(a[k], b[k], m), (var, k, max_rel(a[k], b[k], m))
+
+
+@pytest.mark.parametrize("N", [40, 64])
+def test_mixed_variants_agree_bitwise(N):
+    mesh, s, dt = seeded_case(N, 3, seed=6, oro=True)
+    out = []
+    for var in (0, 1):
+        g = M.Stepper(mesh, dt, precision="mixed", phi_mean=8000.0 * mesh.gravity)
+        g.set_variant(var)
+        assert g.variant == ((0, 32, 32), (1, 32, 16))[var]
+        g.set_state(s)
+        g.step(5)
+        out.append(g.get_state())
+    m = valid_mask(mesh)
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(out[0][k], out[1][k], m), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_autotune_keeps_state_and_caches(precision):
+    mesh, s, dt = seeded_case(24, 3, seed=2, oro=False)
+    kw = dict(phi_mean=8000.0 * mesh.gravity) if precision == "mixed" else {}
+    g = M.Stepper(mesh, dt, precision=precision, **kw)
+    g.set_state(s)
+    g.step(1)
+    before = g.get_state()
+    var, times = g.autotune(reps=3, force=True)
+    nvar = 3 if precision == "fp64" else 2
+    assert 0 <= var < nvar and all(t > 0 for t in times[:nvar]) and times[var] == min(times[:nvar])
+    assert g.variant[0] == var
+    after = g.get_state()
+    m = valid_mask(mesh)
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(before[k], after[k], m), k
+    # a second handle of the same grid reuses the cached choice without timing
+    h = M.Stepper(mesh, dt, precision=precision, **kw)
+    h.set_state(s)
+    var2, times2 = h.autotune(reps=3)
+    assert var2 == var and not any(times2)
+    # stepping after the switch still matches a default-variant handle
+    ref = M.Stepper(mesh, dt, precision=precision, **kw)
+    ref.set_state(s)
+    h.step(3)
+    ref.step(3)
+    a, b = h.get_state(), ref.get_state()
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(a[k], b[k], m), k
+
+
+def test_batch_groups_members_by_variant():
+    mesh, s, dt = seeded_case(20, 3, seed=8, oro=True)
+    members, singles = [], []
+    for var in (0, 1, 2):
+        x = M.Stepper(mesh, dt, precision="fp64")
+        x.set_variant(var)
+        x.set_state(s)
+        members.append(x)
+    y = M.Stepper(mesh, dt, precision="mixed", phi_mean=8000.0 * mesh.gravity)
+    y.set_variant(1)
+    y.set_state(s)
+    members.append(y)
+    M.Batch(members).step(2)
+    for x in members:
+        r = M.Stepper(mesh, dt, precision="fp64" if x is not y else "mixed",
+                      **({} if x is not y else dict(phi_mean=8000.0 * mesh.gravity)))
+        r.set_state(s)
+        r.step(2)
+        a, b = x.get_state(), r.get_state()
+        m = valid_mask(mesh)
+        for k in CHECK_FIELDS:
+            assert bitwise_equal(a[k], b[k], m), k
