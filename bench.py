@@ -154,35 +154,55 @@ def kernel_launch_avg_ms(stepper, steps: int):
 
 
 def e2e_rate(stepper, mesh, state, steps: int, torch):
-    """ccs_set_state + ccs_step(1) + ccs_get_state per step, pinned host buffers."""
+    """Per step: ccs_set_state of the step's input (pinned host -> device), ccs_step(1)
+    and ccs_get_state of its result (device -> pinned host).  Two loops: the async
+    entry points (upload of step k+1 and download of result k overlap the steps; two
+    result buffers in turn), and the synchronous calls one after another."""
     from conformal_cubed_sphere_gb300 import model as M
     pin_in = {k: torch.from_numpy(state[k].copy()).pin_memory() for k in M.STATE_FIELDS}
-    pin_out = {k: torch.empty(mesh.ncell, dtype=torch.float64).pin_memory() for k in M.STATE_FIELDS}
     sin = M.State({k: v.numpy() for k, v in pin_in.items()})
-    sout = M.State({k: v.numpy() for k, v in pin_out.items()})
+    outs = []
+    for _ in range(2):
+        pin_out = {k: torch.empty(mesh.ncell, dtype=torch.float64).pin_memory() for k in M.STATE_FIELDS}
+        outs.append(M.State({k: v.numpy() for k, v in pin_out.items()}))
     # inputs the lane uploads / outputs it downloads
     lane_mixed = stepper._cfg.precision == 1
     n_in = 3 if lane_mixed else 8
     n_out = 8
+    cells = 6 * mesh.N * mesh.N
+    for _ in range(2):  # warm-up of both paths
+        stepper.set_state_async(sin)
+        stepper.step_async(1)
+        stepper.get_state_async(outs[0])
+    stepper.sync()
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        stepper.set_state_async(sin)
+        stepper.step_async(1)
+        stepper.get_state_async(outs[k % 2])
+    stepper.sync()
+    el_async = time.perf_counter() - t0
     t0 = time.perf_counter()
     for _ in range(steps):
         stepper.set_state(sin)
         stepper.step(1)
-        stepper.get_state(sout)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    cells = 6 * mesh.N * mesh.N
+        stepper.get_state(outs[0])
+    el_sync = time.perf_counter() - t0
     nb = mesh.ncell * 8
-    return cells * steps / dt, n_in * nb, n_out * nb
+    return cells * steps / el_async, cells * steps / el_sync, n_in * nb, n_out * nb
 
 
-def cpu_baseline(mesh, state, dt, steps=1):
+def cpu_baseline(mesh, state, dt, seconds=10.0):
+    """The oracle on all host cores, on a sample of about `seconds` of CPU work:
+    as many C384 RK4 steps as one warm-up step says fit (at most 300)."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     orc = O.Oracle.from_mesh(mesh, threads=threads)
     orc.set_state(state.arrays)
+    t0 = time.perf_counter()
     orc.run(dt, 1)  # warm-up (first touch of the work arrays)
+    steps = max(1, min(300, int(seconds / max(time.perf_counter() - t0, 1e-3))))
     t0 = time.perf_counter()
     orc.run(dt, steps)
     el = time.perf_counter() - t0
@@ -202,8 +222,10 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     orc = O.Oracle.from_mesh(mesh, threads=threads)
     orc.set_state(s.arrays)
-    steps = max(1, min(args.steps, 3))
-    warm = max(1, min(args.warmup, 1))
+    # one step = one RK4 step of C384 on all host cores (about 0.1 s on 16 Grace
+    # cores); K and W are honoured up to 600 and 5
+    steps = max(1, min(args.steps, 600))
+    warm = max(1, min(args.warmup, 5))
     orc.run(dt, warm)
     t0 = time.perf_counter()
     orc.run(dt, steps)
@@ -392,11 +414,11 @@ def main():
     mixed2 = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
     mixed2.set_state(s)
     mixed2.autotune()  # the cached choice
-    e2e, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
+    e2e, e2e_sync, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
 
     if rank != 0:
         return
-    cpu = None if args.no_cpu else cpu_baseline(mesh, s, dt, steps=1)
+    cpu = None if args.no_cpu else cpu_baseline(mesh, s, dt)
     line = {
         "metric": "C384 cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_mixed / args.steps,
@@ -411,7 +433,10 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": "mixed_stage_kernel", "kernel_ms_avg": avg_ms,
                      "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind},
-        "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "how": "ccs_set_state_async + ccs_step_async(1) + ccs_get_state_async per step, pinned host "
+                       "buffers, one ccs_sync at the end",
+                "synchronous_calls": e2e_sync},
         "gpu_launches": 4 * args.steps,
         "clocks": sampler.summary(),
         "cpu_baseline": cpu,

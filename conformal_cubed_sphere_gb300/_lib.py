@@ -79,6 +79,8 @@ SIGNATURES = {
     "ccs_destroy": (None, [_vp]),
     "ccs_set_state": (C.c_int, [_vp, C.POINTER(StateView)]),
     "ccs_get_state": (C.c_int, [_vp, C.POINTER(StateView)]),
+    "ccs_set_state_async": (C.c_int, [_vp, C.POINTER(StateView)]),
+    "ccs_get_state_async": (C.c_int, [_vp, C.POINTER(StateView)]),
     "ccs_step": (C.c_int, [_vp, C.c_int]),
     "ccs_step_async": (C.c_int, [_vp, C.c_int]),
     "ccs_sync": (C.c_int, [_vp]),

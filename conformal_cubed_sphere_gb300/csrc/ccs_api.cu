@@ -133,8 +133,9 @@ static void matmul22(const double *X, const double *Y, double *M) {
 static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *mv);
 static int mixed_handle_create(ccs_handle *h);
 static void mixed_handle_destroy(ccs_handle *h);
-static int mixed_set_state(ccs_handle *h, const ccs_state_view *s);
-static int mixed_get_state(ccs_handle *h, ccs_state_view *s);
+static int mixed_set_state(ccs_handle *h, const ccs_state_view *s, bool sync);
+static int mixed_get_state(ccs_handle *h, ccs_state_view *s, bool sync);
+static int mixed_sync(ccs_handle *h);
 static int mixed_step(ccs_handle *h, int nsteps, bool sync);
 static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv);
 static int mixed_diag(ccs_handle *h, double *mass, double *energy);
@@ -476,10 +477,10 @@ void ccs_destroy(ccs_handle *h) {
   delete h;
 }
 
-int ccs_set_state(ccs_handle *h, const ccs_state_view *s) {
+static int set_state_impl(ccs_handle *h, const ccs_state_view *s, bool sync) {
   if (!h || !s || !s->phiG || !s->u || !s->v || !s->phi || !s->uC || !s->vC) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
-  if (h->cfg.precision == CCS_MIXED) return mixed_set_state(h, s);
+  if (h->cfg.precision == CCS_MIXED) return mixed_set_state(h, s, sync);
   const double *src[6] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC};
   double *dst[6] = {h->S[0].phiG, h->S[0].u, h->S[0].v, h->S[0].phi, h->S[0].uC, h->S[0].vC};
   for (int k = 0; k < 6; k++) {
@@ -493,14 +494,17 @@ int ccs_set_state(ccs_handle *h, const ccs_state_view *s) {
     if (rc) return rc;
     h->sphere_valid = true;
   }
-  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  if (sync) CCS_TRY(h, cudaStreamSynchronize(h->stream));
   return CCS_OK;
 }
 
-int ccs_get_state(ccs_handle *h, ccs_state_view *s) {
+int ccs_set_state(ccs_handle *h, const ccs_state_view *s) { return set_state_impl(h, s, true); }
+int ccs_set_state_async(ccs_handle *h, const ccs_state_view *s) { return set_state_impl(h, s, false); }
+
+static int get_state_impl(ccs_handle *h, ccs_state_view *s, bool sync) {
   if (!h || !s) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
-  if (h->cfg.precision == CCS_MIXED) return mixed_get_state(h, s);
+  if (h->cfg.precision == CCS_MIXED) return mixed_get_state(h, s, sync);
   double *dst[6] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC};
   const double *src[6] = {h->S[0].phiG, h->S[0].u, h->S[0].v, h->S[0].phi, h->S[0].uC, h->S[0].vC};
   for (int k = 0; k < 6; k++)
@@ -518,9 +522,12 @@ int ccs_get_state(ccs_handle *h, ccs_state_view *s) {
       if (rc) return rc;
     }
   }
-  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  if (sync) CCS_TRY(h, cudaStreamSynchronize(h->stream));
   return CCS_OK;
 }
+
+int ccs_get_state(ccs_handle *h, ccs_state_view *s) { return get_state_impl(h, s, true); }
+int ccs_get_state_async(ccs_handle *h, ccs_state_view *s) { return get_state_impl(h, s, false); }
 
 int ccs_step(ccs_handle *h, int nsteps) {
   if (!h || nsteps < 0) return CCS_ERR_ARG;
@@ -540,6 +547,7 @@ int ccs_sync(ccs_handle *h) {
   if (!h) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
   CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  if (h->cfg.precision == CCS_MIXED) return mixed_sync(h);
   return CCS_OK;
 }
 
@@ -617,7 +625,15 @@ struct MixedLane {
   float *buf = nullptr;  // S[3] (3 fields each), lo(3), acc(3), tend(3)
   StateMixed S[3]{};
   float *lo[3]{}, *acc[3]{}, *tend[3]{};
-  double *staging = nullptr;  // 8 reference-layout FP64 fields
+  // Reference-layout FP64 staging, double-buffered so that transfers of consecutive
+  // states overlap: in slots hold phi, u, v (3 fields), out slots the 8 exported
+  // fields.  Host-to-device copies run on `cin`, device-to-host copies on `cout`,
+  // the import / export kernels on the handle's stream; events order the slots.
+  double *staging = nullptr;
+  double *stage_in[2]{}, *stage_out[2]{};
+  cudaStream_t cin = nullptr, cout = nullptr;
+  cudaEvent_t in_ready[2]{}, in_free[2]{}, out_ready[2]{}, out_free[2]{};
+  int in_slot = 0, out_slot = 0;
   std::vector<MixedStage> h_stages;
   MixedStage *d_stages = nullptr;
   int n_rk = 0;
@@ -742,7 +758,17 @@ static int mixed_handle_create(ccs_handle *h) {
   for (int k = 0; k < 3; k++) { M->lo[k] = b; b += nf; }
   for (int k = 0; k < 3; k++) { M->acc[k] = b; b += nf; }
   for (int k = 0; k < 3; k++) { M->tend[k] = b; b += nf; }
-  CCS_TRY(h, cudaMalloc(&M->staging, 8 * nref * sizeof(double)));
+  CCS_TRY(h, cudaMalloc(&M->staging, 22 * nref * sizeof(double)));
+  for (int k = 0; k < 2; k++) {
+    M->stage_in[k] = M->staging + 3 * k * nref;
+    M->stage_out[k] = M->staging + (6 + 8 * k) * nref;
+    CCS_TRY(h, cudaEventCreateWithFlags(&M->in_ready[k], cudaEventDisableTiming));
+    CCS_TRY(h, cudaEventCreateWithFlags(&M->in_free[k], cudaEventDisableTiming));
+    CCS_TRY(h, cudaEventCreateWithFlags(&M->out_ready[k], cudaEventDisableTiming));
+    CCS_TRY(h, cudaEventCreateWithFlags(&M->out_free[k], cudaEventDisableTiming));
+  }
+  CCS_TRY(h, cudaStreamCreateWithFlags(&M->cin, cudaStreamNonBlocking));
+  CCS_TRY(h, cudaStreamCreateWithFlags(&M->cout, cudaStreamNonBlocking));
   CCS_TRY(h, cudaMalloc(&h->d_partials, 2 * kDiagBlocks * sizeof(double)));
   int rc = build_work(h, kMxTiles[M->var], &M->d_work, &M->nwork);
   if (rc) return rc;
@@ -812,6 +838,13 @@ static void mixed_handle_destroy(ccs_handle *h) {
   if (!M) return;
   if (M->g_step) cudaGraphExecDestroy(M->g_step);
   if (M->buf) cudaFree(M->buf);
+  if (M->cin) cudaStreamSynchronize(M->cin);
+  if (M->cout) cudaStreamSynchronize(M->cout);
+  for (int k = 0; k < 2; k++)
+    for (cudaEvent_t e : {M->in_ready[k], M->in_free[k], M->out_ready[k], M->out_free[k]})
+      if (e) cudaEventDestroy(e);
+  if (M->cin) cudaStreamDestroy(M->cin);
+  if (M->cout) cudaStreamDestroy(M->cout);
   if (M->staging) cudaFree(M->staging);
   if (M->d_stages) cudaFree(M->d_stages);
   if (M->d_work) cudaFree(M->d_work);
@@ -819,7 +852,7 @@ static void mixed_handle_destroy(ccs_handle *h) {
   h->mixed = nullptr;
 }
 
-static int mixed_set_state(ccs_handle *h, const ccs_state_view *s) {
+static int mixed_set_state(ccs_handle *h, const ccs_state_view *s, bool sync) {
   MixedLane *M = h->mixed;
   const Layout &L = h->L;
   const size_t nref = (size_t)L.nh * L.nh * 6;
@@ -838,32 +871,53 @@ static int mixed_set_state(ccs_handle *h, const ccs_state_view *s) {
     int rc = mixed_build_stages(h);
     if (rc) return rc;
   }
-  double *st = M->staging;
-  CCS_TRY(h, cudaMemcpyAsync(st, s->phi, nref * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  CCS_TRY(h, cudaMemcpyAsync(st + nref, s->u, nref * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  CCS_TRY(h, cudaMemcpyAsync(st + 2 * nref, s->v, nref * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  // copy into the next in slot once the import that last read it has run
+  const int k = M->in_slot;
+  M->in_slot ^= 1;
+  double *st = M->stage_in[k];
+  CCS_TRY(h, cudaStreamWaitEvent(M->cin, M->in_free[k], 0));
+  CCS_TRY(h, cudaMemcpyAsync(st, s->phi, nref * sizeof(double), cudaMemcpyHostToDevice, M->cin));
+  CCS_TRY(h, cudaMemcpyAsync(st + nref, s->u, nref * sizeof(double), cudaMemcpyHostToDevice, M->cin));
+  CCS_TRY(h, cudaMemcpyAsync(st + 2 * nref, s->v, nref * sizeof(double), cudaMemcpyHostToDevice, M->cin));
+  CCS_TRY(h, cudaEventRecord(M->in_ready[k], M->cin));
+  CCS_TRY(h, cudaStreamWaitEvent(h->stream, M->in_ready[k], 0));
   const double a2 = h->cfg.radius * h->cfg.radius;
   CCS_TRY(h, launch_mixed_import(L, st, st + nref, st + 2 * nref, M->phibar, 1. / a2, M->S[0], M->lo[0],
                                  M->lo[1], M->lo[2], h->stream));
-  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  CCS_TRY(h, cudaEventRecord(M->in_free[k], h->stream));
+  if (sync) CCS_TRY(h, cudaStreamSynchronize(h->stream));
   return CCS_OK;
 }
 
-static int mixed_get_state(ccs_handle *h, ccs_state_view *s) {
+static int mixed_get_state(ccs_handle *h, ccs_state_view *s, bool sync) {
   MixedLane *M = h->mixed;
   if (!M->have_phibar) return CCS_ERR_ARG;
   const Layout &L = h->L;
   const size_t nref = (size_t)L.nh * L.nh * 6;
+  // export into the next out slot once the copies that last read it are done
+  const int k = M->out_slot;
+  M->out_slot ^= 1;
   double *out[8];
-  for (int k = 0; k < 8; k++) out[k] = M->staging + k * nref;
+  for (int q = 0; q < 8; q++) out[q] = M->stage_out[k] + q * nref;
   const double a2 = h->cfg.radius * h->cfg.radius;
+  CCS_TRY(h, cudaStreamWaitEvent(h->stream, M->out_free[k], 0));
   CCS_TRY(h, launch_mixed_export(L, M->S[0], M->lo[0], M->lo[1], M->lo[2], h->mesh->m64, M->phibar, a2, out,
                                  h->stream));
+  CCS_TRY(h, cudaEventRecord(M->out_ready[k], h->stream));
+  CCS_TRY(h, cudaStreamWaitEvent(M->cout, M->out_ready[k], 0));
   double *dst[8] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC, s->zonal_wind, s->meridional_wind};
-  for (int k = 0; k < 8; k++)
-    if (dst[k])
-      CCS_TRY(h, cudaMemcpyAsync(dst[k], out[k], nref * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  for (int q = 0; q < 8; q++)
+    if (dst[q])
+      CCS_TRY(h, cudaMemcpyAsync(dst[q], out[q], nref * sizeof(double), cudaMemcpyDeviceToHost, M->cout));
+  CCS_TRY(h, cudaEventRecord(M->out_free[k], M->cout));
+  if (sync) CCS_TRY(h, cudaStreamSynchronize(M->cout));
+  return CCS_OK;
+}
+
+static int mixed_sync(ccs_handle *h) {
+  MixedLane *M = h->mixed;
+  CCS_TRY(h, cudaStreamSynchronize(M->cin));
+  CCS_TRY(h, cudaStreamSynchronize(M->cout));
   return CCS_OK;
 }
 
@@ -918,7 +972,8 @@ static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv) {
   const size_t nref = (size_t)L.nh * L.nh * 6;
   CCS_TRY(h, launch_mixed_stage(M->var, M->d_stages + M->n_rk, M->d_work, M->nwork, M->grid, h->stream));
   const double a2 = h->cfg.radius * h->cfg.radius;
-  double *o = M->staging;
+  CCS_TRY(h, cudaStreamSynchronize(M->cout));  // no copy may still read the out slots
+  double *o = M->stage_out[0];
   CCS_TRY(h, launch_mixed_tend_export(L, M->tend[0], M->tend[1], M->tend[2], h->mesh->m64, a2, o, o + nref,
                                       o + 2 * nref, h->stream));
   double *dst[3] = {tp, tu, tv};

@@ -204,6 +204,7 @@ class Stepper:
                        e_dissipation=e_dissipation, device=device, dx=mesh.dx, dy=mesh.dy, dt=self.dt,
                        radius=mesh.radius, gravity=mesh.gravity, omega=mesh.omega, phi_mean=phi_mean)
         self._cfg = cfg
+        self._pending = []  # host arrays of async transfers, held until sync()
         h = C.c_void_p()
         lib = L.lib()
         if share_with is None:
@@ -259,6 +260,19 @@ class Stepper:
         L.check(L.lib().ccs_get_state(self.handle, C.byref(sv)), "ccs_get_state", self.handle)
         return out
 
+    def set_state_async(self, s: State):
+        """ccs_set_state_async: the arrays of `s` are held until sync()."""
+        sv = s.view()
+        L.check(L.lib().ccs_set_state_async(self.handle, C.byref(sv)), "ccs_set_state_async", self.handle)
+        self._pending.append(s)
+
+    def get_state_async(self, out: State) -> State:
+        """ccs_get_state_async into `out` (valid after sync())."""
+        sv = out.view()
+        L.check(L.lib().ccs_get_state_async(self.handle, C.byref(sv)), "ccs_get_state_async", self.handle)
+        self._pending.append(out)
+        return out
+
     def step(self, nsteps: int = 1):
         L.check(L.lib().ccs_step(self.handle, int(nsteps)), "ccs_step", self.handle)
 
@@ -267,6 +281,7 @@ class Stepper:
 
     def sync(self):
         L.check(L.lib().ccs_sync(self.handle), "ccs_sync", self.handle)
+        self._pending.clear()
 
     def spatial_operator(self):
         n = self.mesh.ncell

@@ -150,6 +150,16 @@ int ccs_step(ccs_handle *h, int nsteps);
 int ccs_step_async(ccs_handle *h, int nsteps);
 int ccs_sync(ccs_handle *h);
 
+/* ccs_set_state / ccs_get_state without the final wait: the copies and conversion
+ * kernels are enqueued in order with the handle's steps, and the host arrays must
+ * stay valid (and, for set, unchanged) until ccs_sync returns.  On the mixed lane
+ * the copies run on two copy streams with double-buffered device staging, so a loop
+ * of set_async / step_async / get_async overlaps the upload of one state and the
+ * download of the previous result with the step in between; pass page-locked host
+ * arrays for the copies to be asynchronous.  No counterpart in the reference. */
+int ccs_set_state_async(ccs_handle *h, const ccs_state_view *s);
+int ccs_get_state_async(ccs_handle *h, ccs_state_view *s);
+
 /* Selects the spatial operator of the handle's steps (default CCS_OP_WENO): the
  * choice the reference makes at build time by compiling one of its four
  * spatial_operators_mod sources.  FP64 lane only (CCS_ERR_UNSUPPORTED on the mixed

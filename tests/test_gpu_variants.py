@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("var", [0, 1, 2])
-@pytest.mark.parametrize("N", [20, 33])
+@pytest.mark.parametrize("N", [20, 34])  # partial tiles for every shape; even N (no cell on a pole)
 def test_fp64_variants_bitwise_against_oracle(var, N):
     mesh, s, dt = seeded_case(N, 3, seed=4, oro=True)
     g = M.Stepper(mesh, dt, precision="fp64")

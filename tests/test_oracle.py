@@ -270,3 +270,26 @@ def test_rk4_combination_matches_four_stage_formula():
     im = mesh.interior_mask()
     comb = (k[0] + 2.0 * k[1] + 2.0 * k[2] + k[3]) / 6.0
     assert np.array_equal(new["phiG"][im], (s["phiG"] + dt * comb)[im])
+
+
+def test_pole_cell_inverse_follows_the_reference_formula():
+    """Odd N puts a cell centre on each pole, where read_mesh replaces A^-1 by its
+    'analytical approximation' (io_mod.F90:190-210): the lon rotation times the
+    radius.  The metric derivation keeps that formula as written.  (A^-1 elsewhere
+    scales as 1/radius, so the pole cell's covariant wind comes out a^2 times too
+    large and an odd-N run of the reference step blows up in its first step; even N
+    has no pole cell.)"""
+    N, h = 5, 3
+    mesh = M.Mesh(N, h)
+    IA = mesh.matrixIA.reshape((2, 2, N + 2 * h, N + 2 * h, 6), order="F")
+    lon = mesh.field(mesh.lon)
+    c = h + N // 2
+    for p, sign in ((4, 1.0), (5, -1.0)):  # panel 5 north pole, panel 6 south pole
+        lo = lon[c, c, p]
+        if sign > 0:
+            want = np.array([[np.cos(lo), -np.sin(lo)], [np.sin(lo), np.cos(lo)]]) * mesh.radius
+        else:
+            want = np.array([[-np.cos(lo), np.sin(lo)], [np.sin(lo), np.cos(lo)]]) * mesh.radius
+        assert np.allclose(IA[:, :, c, c, p], want, rtol=1e-15, atol=0)
+    # an off-pole cell: A^-1 is the inverse of A, of order 1/radius
+    assert np.max(np.abs(IA[:, :, c + 1, c, 4])) < 1e-5
