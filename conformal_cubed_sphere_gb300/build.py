@@ -4,7 +4,9 @@ Every translation unit is compiled in parallel with nvcc and linked into one
 shared library with the CUDA runtime linked statically.  Host code is compiled
 with ``-ffp-contract=off``: the FP64 set-up arithmetic (metric products, halo
 transforms) must not be fused on aarch64 hosts, where gcc contracts by default.
-The FP64 parity kernels are compiled with ``-fmad=false`` for the same reason.
+The FP64 parity kernels are compiled with ``-fmad=false`` for the same reason, and
+so is the mixed lane, whose FMAs are all written out: the tile-shape variants of its
+stage kernel then round identically.
 """
 from __future__ import annotations
 
@@ -24,7 +26,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # (source, extra flags)
 UNITS = [
     ("ccs_fp64.cu", ["-fmad=false"]),
-    ("ccs_mixed.cu", []),
+    ("ccs_mixed.cu", ["-fmad=false"]),  # FMAs explicit: every tile variant rounds alike
     ("ccs_api.cu", []),
     ("ccs_host.cpp", []),
     ("ccs_noalloc.cu", []),

@@ -149,6 +149,17 @@ __device__ __forceinline__ void weno_d2(float2 d0, float2 d1, float2 d2, float2 
   }
 }
 
+// 60 dx times the 6th-order centred derivative (spatial_operators_mod.F90:165,169)
+// of the values f[-3s .. 3s], the FMAs written out so that every build rounds the
+// same way
+__device__ __forceinline__ float diff6(const float *f, int s) {
+  float t = fmaf(9.f, f[-2 * s], -f[-3 * s]);
+  t = fmaf(-45.f, f[-s], t);
+  t = fmaf(45.f, f[s], t);
+  t = fmaf(-9.f, f[2 * s], t);
+  return t + f[3 * s];
+}
+
 template <class T>
 struct SmemMx {
   MixedStage st;  // this work item's stage descriptor
@@ -227,9 +238,9 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
       const int fg = startg + fi;    // global index of the cell left of / below the face
       if (fg <= L.N) {
         const float uB = 0.5f * (pU + uc);
-        const float pB = phibar + 0.5f * (pH + hc);
+        const float pB = fmaf(0.5f, pH + hc, phibar);
         const float lm = fabsf(uB) + sqrtf(fmaxf(lam_cur * pB, 0.f));
-        const float gF = 0.5f * (dF1 + pDFp + DFm - lm * (dP1 + DPm - pDPp));
+        const float gF = 0.5f * fmaf(-lm, dP1 + DPm - pDPp, dF1 + pDFp + DFm);
         const float gE = 0.5f * (dE1 + pDEp + DEm);
         if (XDIR) {
           S.gx[0][line][fi] = gF;
@@ -336,10 +347,8 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       const float divy = (S.gy[0][lj + 1][li] - S.gy[0][lj][li] + (S.G[r] - S.G[r - SP])) * st.rdy;
       const float dEdy = (S.gy[1][lj + 1][li] - S.gy[1][lj][li] + (S.E[r] - S.E[r - SP])) * st.rdy;
       const float *vv = S.v + r, *uu = S.u + r;
-      const float dvdx = (-vv[-3] + 9.f * vv[-2] - 45.f * vv[-1] + 45.f * vv[1] - 9.f * vv[2] + vv[3]) * st.rdx60;
-      const float dudy = (-uu[-3 * SP] + 9.f * uu[-2 * SP] - 45.f * uu[-SP] + 45.f * uu[SP] - 9.f * uu[2 * SP] +
-                          uu[3 * SP]) *
-                         st.rdy60;
+      const float dvdx = diff6(vv, 1) * st.rdx60;
+      const float dudy = diff6(uu, SP) * st.rdy60;
       const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
       const float vort = dvdx - dudy + __ldg(st.m.fs + c);
       const float tp = -(divx + divy) * __ldg(st.m.inv_s + cs);
@@ -352,18 +361,20 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         continue;
       }
       const float y0p = st.y0hp[c], y0u = st.y0u[c], y0v = st.y0v[c];
-      float ip, iu, iv;  // increments to Y0
-      bool fin = false;
+      float ip, iu, iv;  // increments to Y0 (Y = Y0 + c1 k fused where the stage is linear)
+      bool fin = false, lin = false;
       switch (st.kind) {
         case K_RK4_1:
           st.acchp[c] = tp; st.accu[c] = tu; st.accv[c] = tv;
-          ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
+          ip = tp; iu = tu; iv = tv;
+          lin = true;
           break;
         case K_RK4_2:
           st.acchp[c] = fmaf(2.f, tp, st.acchp[c]);
           st.accu[c] = fmaf(2.f, tu, st.accu[c]);
           st.accv[c] = fmaf(2.f, tv, st.accv[c]);
-          ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
+          ip = tp; iu = tu; iv = tv;
+          lin = true;
           break;
         case K_RK4_4: {
           const float k6 = st.c1 * (1.f / 6.f);
@@ -372,7 +383,8 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
           break;
         }
         case K_RK3_1:
-          ip = st.c1 * tp; iu = st.c1 * tu; iv = st.c1 * tv;
+          ip = tp; iu = tu; iv = tv;
+          lin = true;
           break;
         case K_RK3_2:
           ip = fmaf(0.25f, st.in.hp[c] - y0p, st.c1 * tp);
@@ -403,6 +415,8 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         }
         np = out[0]; nu = out[1]; nv = out[2];
         st.lohp[c] = lo[0]; st.lou[c] = lo[1]; st.lov[c] = lo[2];
+      } else if (lin) {
+        np = fmaf(st.c1, ip, y0p); nu = fmaf(st.c1, iu, y0u); nv = fmaf(st.c1, iv, y0v);
       } else {
         np = y0p + ip; nu = y0u + iu; nv = y0v + iv;
       }
@@ -442,8 +456,8 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         const int64_t d = st.m.push[e];
         const double *X = st.m.xf + 4 * e;
         const float np = st.out.hp[c], nu = st.out.u[c], nv = st.out.v[c];
-        const double ud = X[0] * (double)nu + X[1] * (double)nv;
-        const double vd = X[2] * (double)nu + X[3] * (double)nv;
+        const double ud = fma(X[0], (double)nu, X[1] * (double)nv);
+        const double vd = fma(X[2], (double)nu, X[3] * (double)nv);
         st.out.hp[d] = np;
         st.out.u[d] = (float)ud;
         st.out.v[d] = (float)vd;
