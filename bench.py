@@ -343,6 +343,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="c384", choices=["c384", "ensemble", "uneven"])
     ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--tile-variant", type=int, default=-1,
+                    help="mixed-lane tile variant of the C384 run (-1: autotuner)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=5)
@@ -373,7 +375,11 @@ def main():
     phibar = 8000.0 * mesh.gravity
     mixed = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
     mixed.set_state(s)
-    tuned = {"mixed": mixed.autotune(reps=5)}
+    if args.tile_variant >= 0:  # fixed (profiling runs: timing under a profiler is not representative)
+        mixed.set_variant(args.tile_variant)
+        tuned = {"mixed": (args.tile_variant, [])}
+    else:
+        tuned = {"mixed": mixed.autotune(reps=5)}
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
     mixed.step(max(args.warmup, 3))
     torch.cuda.synchronize()
@@ -413,7 +419,7 @@ def main():
     e2e_steps = max(3, min(20, args.steps))
     mixed2 = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
     mixed2.set_state(s)
-    mixed2.autotune()  # the cached choice
+    mixed2.set_variant(mixed.variant[0])
     e2e, e2e_sync, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
 
     if rank != 0:

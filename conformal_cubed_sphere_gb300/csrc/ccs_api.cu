@@ -1043,24 +1043,28 @@ static int set_variant(ccs_handle *h, int var) {
   return CCS_OK;
 }
 
-// Mean time of one launch of the handle's first RK stage with its current variant.
-// That stage reads the state and writes only stage scratch (the next stage's input
-// and the RK accumulator), so timing it leaves the state unchanged.
-static int time_first_stage(ccs_handle *h, int reps, double *us) {
+// Mean time of one stage launch with the handle's current variant, over the RK
+// stages before the last one, in step order.  Those stages read the state and
+// write only stage scratch (the next stage's input and the RK accumulator); the
+// last stage, which writes the state, is the only one left out, so timing leaves
+// the state unchanged.
+static int time_stages(ccs_handle *h, int reps, double *us) {
+  const bool mx = h->cfg.precision == CCS_MIXED;
+  const int nst = (mx ? h->mixed->n_rk : h->n_rk) - 1;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   CCS_TRY(h, cudaEventCreate(&e0));
   CCS_TRY(h, cudaEventCreate(&e1));
-  auto launch = [&]() -> cudaError_t {
-    if (h->cfg.precision == CCS_MIXED) {
+  auto launch = [&](int k) -> cudaError_t {
+    if (mx) {
       MixedLane *M = h->mixed;
-      return launch_mixed_stage(M->var, M->d_stages, M->d_work, M->nwork, M->grid, h->stream);
+      return launch_mixed_stage(M->var, M->d_stages + k, M->d_work, M->nwork, M->grid, h->stream);
     }
-    return launch_f64_stage(h->var, h->d_stages, h->d_work, h->nwork, h->grid, h->stream);
+    return launch_f64_stage(h->var, h->d_stages + k, h->d_work, h->nwork, h->grid, h->stream);
   };
-  cudaError_t e = launch();  // warm-up
+  cudaError_t e = launch(0);  // warm-up
   for (int r = 0; r < reps && e == cudaSuccess; r++) {
     if (r == 0) e = cudaEventRecord(e0, h->stream);
-    if (e == cudaSuccess) e = launch();
+    for (int k = 0; k < nst && e == cudaSuccess; k++) e = launch(k);
   }
   if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -1069,7 +1073,7 @@ static int time_first_stage(ccs_handle *h, int reps, double *us) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CCS_TRY(h, e);
-  *us = 1e3 * ms / reps;
+  *us = 1e3 * ms / (reps * nst);
   return CCS_OK;
 }
 
@@ -1110,7 +1114,7 @@ extern "C" int ccs_autotune(ccs_handle *h, int reps, int force, int *chosen, dou
       int rc = set_variant(h, v);
       if (rc) return rc;
       double us = 0.;
-      rc = time_first_stage(h, reps, &us);
+      rc = time_stages(h, reps, &us);
       if (rc) return rc;
       if (times_us) times_us[v] = us;
       if (best < 0 || us < best_us) {

@@ -171,9 +171,9 @@ int ccs_set_operator(ccs_handle *h, int op);
  * Each lane's stage kernel comes in tile-shape variants (cells per work item):
  * FP64 lane 0: 32x8, 1: 16x16, 2: 64x4; mixed lane 0: 32x32, 1: 32x16.  Every
  * variant computes the same per-cell arithmetic, so results do not depend on the
- * choice.  ccs_autotune times the handle's first RK stage (which writes only stage
- * scratch, so the state is unchanged) `reps` times with each variant after one
- * warm-up launch and keeps the fastest; the choice is cached per (device, lane, N,
+ * choice.  ccs_autotune times the handle's RK stages before the last one (they write
+ * only stage scratch, so the state is unchanged), `reps` rounds with each variant
+ * after one warm-up launch, and keeps the fastest mean stage time; the choice is cached per (device, lane, N,
  * halo) for the process, and later calls with force = 0 reuse it without timing.
  * The state must be set first.  chosen (may be NULL) receives the variant,
  * times_us (may be NULL, CCS_MAX_VARIANTS entries) the mean launch times in
