@@ -21,6 +21,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libccs_gpu.so"
+DRIVER = BUILD / "ccsm_gpu"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # (source, extra flags)
@@ -53,7 +54,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     """Compile and link; returns the library path.  Skips work when up to date."""
     BUILD.mkdir(exist_ok=True)
     srcs = [CSRC / s for s, _ in UNITS]
-    deps = srcs + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "ccs_gpu.h", Path(__file__)]
+    deps = srcs + list(CSRC.glob("*.h")) + [CSRC / "ccsm_gpu.cpp", PKG.parent / "include" / "ccs_gpu.h",
+                                            Path(__file__)]
     if not force and LIB.exists():
         t = LIB.stat().st_mtime
         if all(d.stat().st_mtime <= t for d in deps):
@@ -82,6 +84,13 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the model program over the C ABI (a C++ host driver linked against the library)
+    drv = BUILD / "ccsm_gpu"
+    cmd = [nvcc, "-O2", "-std=c++17", "-x", "c++", "-Xcompiler", "-ffp-contract=off", f"-I{PKG.parent / 'include'}",
+           str(CSRC / "ccsm_gpu.cpp"), f"-L{BUILD}", "-lccs_gpu", "-Xlinker", "-rpath,$ORIGIN", "-o", str(drv)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
