@@ -651,13 +651,17 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
   const double a2 = h->cfg.radius * h->cfg.radius;
   const size_t nf = (size_t)L.field, np = (size_t)L.panel;
   const size_t nref = (size_t)nh * nh * 6;
-  // shared: s inv_s lamx lamy (one panel each) + ig as float4; per panel: phis fs
-  const size_t nfloat = 8 * np + 2 * nf;  // s, inv_s, lamx, lamy, ig (4 per cell), phis, fs
+  // shared: s inv_s lamx lamy (one panel each; the face metrics followed by 32 zero
+  // rows that the stage kernel's one-face-ahead prefetch may read in partial tiles)
+  // + ig as float4; per panel: phis fs
+  const size_t pad = 32 * (size_t)L.pitch;  // a multiple of 4 floats: ig stays 16-byte aligned
+  const size_t o_lamx = 2 * np, o_lamy = 3 * np + pad, o_ig = 4 * np + 2 * pad;
+  const size_t nfloat = o_ig + 4 * np + 2 * nf;  // s, inv_s, lamx, lamy, ig (4 per cell), phis, fs
   CCS_TRY(h, cudaMalloc(&dm->buf32, nfloat * sizeof(float)));
   std::vector<float> hb(nfloat, 0.f);
-  float *sh_s = hb.data(), *sh_inv = hb.data() + np, *sh_lamx = hb.data() + 2 * np, *sh_lamy = hb.data() + 3 * np;
-  float *sh_ig = hb.data() + 4 * np;  // interleaved (11, 12, 21, 22), 16-byte aligned (np % 4 == 0)
-  float *phs = hb.data() + 8 * np, *fs = phs + nf;
+  float *sh_s = hb.data(), *sh_inv = hb.data() + np, *sh_lamx = hb.data() + o_lamx, *sh_lamy = hb.data() + o_lamy;
+  float *sh_ig = hb.data() + o_ig;  // interleaved (11, 12, 21, 22), 16-byte aligned (np % 4 == 0)
+  float *phs = hb.data() + o_ig + 4 * np, *fs = phs + nf;
   for (int p = 0; p < 6; p++)
     for (int j = 1 - hh; j <= N + hh; j++)
       for (int i = 1 - hh; i <= N + hh; i++) {
@@ -730,11 +734,11 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
   dm->xf = dxf;
   dm->mm.s = dm->buf32;
   dm->mm.inv_s = dm->buf32 + np;
-  dm->mm.lamx = dm->buf32 + 2 * np;
-  dm->mm.lamy = dm->buf32 + 3 * np;
-  dm->mm.ig = reinterpret_cast<const float4 *>(dm->buf32 + 4 * np);
-  dm->mm.phis = dm->buf32 + 8 * np;
-  dm->mm.fs = dm->buf32 + 8 * np + nf;
+  dm->mm.lamx = dm->buf32 + o_lamx;
+  dm->mm.lamy = dm->buf32 + o_lamy;
+  dm->mm.ig = reinterpret_cast<const float4 *>(dm->buf32 + o_ig);
+  dm->mm.phis = dm->buf32 + o_ig + 4 * np;
+  dm->mm.fs = dm->buf32 + o_ig + 4 * np + nf;
   dm->mm.xf = dxf;
   dm->mm.push = dm->push;
   (void)nref;

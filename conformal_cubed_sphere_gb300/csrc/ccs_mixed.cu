@@ -65,7 +65,8 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
   // unconditionally and selected, so no branch diverges
   const float sa = fmaf(1.f / 3.f, p1, (2.f / 3.f) * p2), sb = fmaf(2.f / 3.f, p2, (1.f / 3.f) * p3);
   const float ta = fmaf(1.f / 3.f, m1, (2.f / 3.f) * m2), tb = fmaf(2.f / 3.f, m2, (1.f / 3.f) * m3);
-  const bool lo40 = t40 <= mn, lo41 = t41 <= mn, hi40 = t40 > mn, hi41 = t41 > mn;
+  // (the reference's t > mn tests are the complements of t <= mn for finite data)
+  const bool lo40 = t40 <= mn, lo41 = t41 <= mn, hi40 = !lo40, hi41 = !lo41;
   const bool lt40 = t40 < mn, lt41 = t41 < mn;
   {  // "+" weights
     const float a1 = fmaf(0.1f, r1, 0.1f), a2 = fmaf(0.6f, r2, 0.6f), a3 = fmaf(0.3f, r3, 0.3f);
@@ -122,7 +123,7 @@ __device__ __forceinline__ void weno_d2(float2 d0, float2 d1, float2 d2, float2 
     const float x1 = __fdividef(t5, q ? e1.y : e1.x), x2 = __fdividef(t5, q ? e2.y : e2.x),
                 x3 = __fdividef(t5, q ? e3.y : e3.x);
     if (q) { r1.y = x1; r2.y = x2; r3.y = x3; } else { r1.x = x1; r2.x = x2; r3.x = x3; }
-    lo40[q] = t40 <= mn; lo41[q] = t41 <= mn; hi40[q] = t40 > mn; hi41[q] = t41 > mn;
+    lo40[q] = t40 <= mn; lo41[q] = t41 <= mn; hi40[q] = !lo40[q]; hi41[q] = !lo41[q];
     lt40[q] = t40 < mn; lt41[q] = t41 < mn;
   }
   {  // "+" weights
@@ -203,18 +204,19 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
   float Flast = Fv[3], Elast = Ev[3], slast = sv[3], qlast = q3;
   float hc = hv[2], hc1 = hv[3];  // hs at c and c+1
   float pDFp = 0.f, pDEp = 0.f, pDPp = 0.f, pU = 0.f, pH = 0.f;
-  // face wave-speed metric, fetched one face ahead of its use (the index is clamped
-  // into the panel so the prefetch never leaves the array)
-  auto lam_at = [&](int fi) -> float {
-    int fg = startg + fi;
-    fg = fg < 0 ? 0 : (fg > L.N ? L.N : fg);
-    return __ldg(lam + (XDIR ? L.idx(fg, lineg, 0) : L.idx(lineg, fg, 0)));
-  };
-  float lam_next = lam_at(f0);
+  // face wave-speed metric, fetched one face ahead of its use by walking a pointer
+  // along the line; faces of a partial tile beyond N are read (and not used) from
+  // the 32 padding rows the metric arrays carry after each panel block
+  const float *lp = lam + (XDIR ? L.idx(startg + f0, lineg, 0) : L.idx(lineg, startg + f0, 0));
+  const int lstride = XDIR ? 1 : L.pitch;
+  float lam_next = __ldg(lp);
   for (int k = 0; k <= NFACE; k++) {
     const int ci = f0 + k;
     const float lam_cur = lam_next;
-    if (k > 0 && k < NFACE) lam_next = lam_at(ci);
+    if (k > 0 && k < NFACE) {
+      lp += lstride;
+      lam_next = __ldg(lp);
+    }
     const int on = base + (ci + 2) * stp;  // cell c+2
     const float Fn = Qflux[on], En = S.E[on], hn = S.hs[on], sn = S.s[on];
     const float qn = hn * sn;
