@@ -113,6 +113,8 @@ static int validate_config(const ccs_config *c) {
   if (c->scheme != CCS_RK4 && c->scheme != CCS_RK3_TVD) return CCS_ERR_ARG;
   if (c->precision != CCS_FP64 && c->precision != CCS_MIXED) return CCS_ERR_ARG;
   if (c->e_dissipation != CCS_EDISS_ZERO && c->e_dissipation != CCS_EDISS_RECONSTRUCT) return CCS_ERR_ARG;
+  // the mixed lane implements the reference's data flow only (never-written face slots read as 0)
+  if (c->precision == CCS_MIXED && c->e_dissipation != CCS_EDISS_ZERO) return CCS_ERR_UNSUPPORTED;
   if (!(c->dx > 0.) || !(c->dy > 0.) || !(c->dt > 0.) || !(c->radius > 0.) || !(c->gravity > 0.))
     return CCS_ERR_ARG;
   if (!std::isfinite(c->dx) || !std::isfinite(c->dy) || !std::isfinite(c->dt) || !std::isfinite(c->omega))

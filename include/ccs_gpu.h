@@ -61,7 +61,8 @@ enum {
  * u_ext / v_ext that the reference never writes (u is reconstructed only at
  * y-faces, v only at x-faces).  ZERO reads them as 0.0, i.e. E at a face is the
  * plain average of its two reconstructions (what a freshly zeroed scratch gives).
- * RECONSTRUCT fills them with WENO reconstructions of u at x-faces and v at y-faces. */
+ * RECONSTRUCT fills them with WENO reconstructions of u at x-faces and v at y-faces
+ * (FP64 lane; ccs_init returns CCS_ERR_UNSUPPORTED for it on the mixed lane). */
 enum { CCS_EDISS_ZERO = 0, CCS_EDISS_RECONSTRUCT = 1 };
 
 /* spatial operator.  The reference ships four interchangeable modules of the same
