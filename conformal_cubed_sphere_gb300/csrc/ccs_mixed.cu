@@ -335,9 +335,34 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         if (i0 + line <= N) tile_line<false>(S, S.G, S.vC, st.m.lamy, L, line, f0, nface, j0 - 1, i0 + line);
       }
     }
+    // Global operands of phase 3 for this thread's four cells, loaded before the
+    // barrier so their latency overlaps the wait for the slowest line segment:
+    // f s, 1/s, Y0, the accumulator (or the stage input's hp for RK3) and the
+    // compensation terms, as the stage kind needs them (uniform over the CTA).
+    const int kind = st.kind;
+    const bool need_acc = kind == K_RK4_2 || kind == K_RK4_4;
+    const bool need_in = kind == K_RK3_2 || kind == K_RK3_3;
+    const bool need_lo = kind == K_RK4_4 || kind == K_RK3_3;
+    float q_fs[4], q_is[4], q_y0[4][3], q_a[4][3], q_lo[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int i = i0 + lane, j = j0 + warp + (NT / 32) * k;
+      q_fs[k] = q_is[k] = 0.f;
+#pragma unroll
+      for (int q = 0; q < 3; q++) q_y0[k][q] = q_a[k][q] = q_lo[k][q] = 0.f;
+      if (i > N || j > N) continue;
+      const int64_t c = L.idx(i, j, p);
+      q_fs[k] = __ldg(st.m.fs + c);
+      q_is[k] = __ldg(st.m.inv_s + L.idx(i, j, 0));
+      if (kind == K_TEND) continue;
+      q_y0[k][0] = st.y0hp[c]; q_y0[k][1] = st.y0u[c]; q_y0[k][2] = st.y0v[c];
+      if (need_acc) { q_a[k][0] = st.acchp[c]; q_a[k][1] = st.accu[c]; q_a[k][2] = st.accv[c]; }
+      if (need_in) q_a[k][0] = st.in.hp[c];
+      if (need_lo) { q_lo[k][0] = st.lohp[c]; q_lo[k][1] = st.lou[c]; q_lo[k][2] = st.lov[c]; }
+    }
     __syncthreads();
 
-    // ---- phase 3: tendencies, stage update, ghost push -------------------------
+    // ---- phase 3: tendencies, stage update ---------------------------------------
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       const int li = lane, lj = warp + (NT / 32) * k;
@@ -351,36 +376,36 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       const float *vv = S.v + r, *uu = S.u + r;
       const float dvdx = diff6(vv, 1) * st.rdx60;
       const float dudy = diff6(uu, SP) * st.rdy60;
-      const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
-      const float vort = dvdx - dudy + __ldg(st.m.fs + c);
-      const float tp = -(divx + divy) * __ldg(st.m.inv_s + cs);
+      const int64_t c = L.idx(i, j, p);
+      const float vort = dvdx - dudy + q_fs[k];
+      const float tp = -(divx + divy) * q_is[k];
       const float tu = fmaf(vort, S.vC[r], -dEdx * st.inv_a2);
       const float tv = fmaf(-vort, S.uC[r], -dEdy * st.inv_a2);
-      if (st.kind == K_TEND) {
+      if (kind == K_TEND) {
         st.thp[c] = tp;
         st.tu[c] = tu;
         st.tv[c] = tv;
         continue;
       }
-      const float y0p = st.y0hp[c], y0u = st.y0u[c], y0v = st.y0v[c];
+      const float y0p = q_y0[k][0], y0u = q_y0[k][1], y0v = q_y0[k][2];
       float ip, iu, iv;  // increments to Y0 (Y = Y0 + c1 k fused where the stage is linear)
       bool fin = false, lin = false;
-      switch (st.kind) {
+      switch (kind) {
         case K_RK4_1:
           st.acchp[c] = tp; st.accu[c] = tu; st.accv[c] = tv;
           ip = tp; iu = tu; iv = tv;
           lin = true;
           break;
         case K_RK4_2:
-          st.acchp[c] = fmaf(2.f, tp, st.acchp[c]);
-          st.accu[c] = fmaf(2.f, tu, st.accu[c]);
-          st.accv[c] = fmaf(2.f, tv, st.accv[c]);
+          st.acchp[c] = fmaf(2.f, tp, q_a[k][0]);
+          st.accu[c] = fmaf(2.f, tu, q_a[k][1]);
+          st.accv[c] = fmaf(2.f, tv, q_a[k][2]);
           ip = tp; iu = tu; iv = tv;
           lin = true;
           break;
         case K_RK4_4: {
           const float k6 = st.c1 * (1.f / 6.f);
-          ip = k6 * (st.acchp[c] + tp); iu = k6 * (st.accu[c] + tu); iv = k6 * (st.accv[c] + tv);
+          ip = k6 * (q_a[k][0] + tp); iu = k6 * (q_a[k][1] + tu); iv = k6 * (q_a[k][2] + tv);
           fin = true;
           break;
         }
@@ -389,12 +414,12 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
           lin = true;
           break;
         case K_RK3_2:
-          ip = fmaf(0.25f, st.in.hp[c] - y0p, st.c1 * tp);
+          ip = fmaf(0.25f, q_a[k][0] - y0p, st.c1 * tp);
           iu = fmaf(0.25f, S.u[r] - y0u, st.c1 * tu);
           iv = fmaf(0.25f, S.v[r] - y0v, st.c1 * tv);
           break;
         default:  // K_RK3_3
-          ip = fmaf(2.f / 3.f, st.in.hp[c] - y0p, st.c1 * tp);
+          ip = fmaf(2.f / 3.f, q_a[k][0] - y0p, st.c1 * tp);
           iu = fmaf(2.f / 3.f, S.u[r] - y0u, st.c1 * tu);
           iv = fmaf(2.f / 3.f, S.v[r] - y0v, st.c1 * tv);
           fin = true;
@@ -403,7 +428,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       float np, nu, nv;
       if (fin) {
         // compensated update of the step-to-step state (TwoSum)
-        float lo[3] = {st.lohp[c], st.lou[c], st.lov[c]};
+        float lo[3] = {q_lo[k][0], q_lo[k][1], q_lo[k][2]};
         const float hi[3] = {y0p, y0u, y0v};
         const float inc[3] = {ip, iu, iv};
         float out[3];
