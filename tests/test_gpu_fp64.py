@@ -229,3 +229,14 @@ def test_c192_1000_steps_with_orography_bitwise():
     m = valid_mask(mesh)
     for k in CHECK_FIELDS:
         assert bitwise_equal(g[k], o[k], m), (k, max_rel(g[k], o[k], m))
+
+
+def test_rk3_reconstruct_halo5_60_steps_bitwise():
+    """RK3-TVD with the E-reconstruction option at halo 5, 60 steps of C24."""
+    mesh, s, dt, gpu, orc = _pair(24, 5, seed=13, oro=True, scheme="RK3_TVD", ediss=1)
+    gpu.step(60)
+    orc.run(dt, 60, "RK3_TVD")
+    g, o = gpu.get_state(), orc.get_state()
+    m = valid_mask(mesh)
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(g[k], o[k], m), (k, max_rel(g[k], o[k], m))
