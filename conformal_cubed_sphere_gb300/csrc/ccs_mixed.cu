@@ -266,6 +266,11 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
 #ifndef CCS_MIXED_MIN_CTAS
 #define CCS_MIXED_MIN_CTAS 3
 #endif
+// halo'd-tile cells each thread loads per round in phase 1 (loads in flight)
+#ifndef CCS_MIXED_P1_UNROLL
+#define CCS_MIXED_P1_UNROLL 2
+#endif
+constexpr int kP1Unroll = CCS_MIXED_P1_UNROLL;
 
 template <class T>
 __global__ void __launch_bounds__(T::NT, CCS_MIXED_MIN_CTAS * 32 / T::TY)
@@ -295,7 +300,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       const float phibar = st.phibar, ha2 = 0.5f * st.a2;
       const float *__restrict__ ihp = st.in.hp, *__restrict__ iu = st.in.u, *__restrict__ iv = st.in.v;
       const MeshMixed m = st.m;
-#pragma unroll 2
+#pragma unroll kP1Unroll
       for (int r = tid; r < RX * RY; r += NT) {
         const int li = r % RX, lj = r / RX;
         const int i = i0 - 3 + li, j = j0 - 3 + lj;
