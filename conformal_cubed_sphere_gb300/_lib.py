@@ -86,6 +86,7 @@ SIGNATURES = {
     "ccs_sync": (C.c_int, [_vp]),
     "ccs_spatial_operator": (C.c_int, [_vp, _dp, _dp, _dp]),
     "ccs_set_operator": (C.c_int, [_vp, C.c_int]),
+    "ccs_check_state": (C.c_int, [_vp, C.POINTER(C.c_int64)]),
     "ccs_autotune": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_int), _dp]),
     "ccs_set_variant": (C.c_int, [_vp, C.c_int]),
     "ccs_get_variant": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),

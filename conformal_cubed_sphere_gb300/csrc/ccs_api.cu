@@ -2,6 +2,7 @@
 // descriptors, CUDA-graph capture of a step, state transfer and diagnostics.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -20,6 +21,27 @@ using namespace ccs;
 namespace {
 
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// Health check: counts interior cells whose depth is not positive (NaN included) or
+// whose covariant wind is not finite.  phi = phi0 + hp[c] (FP64 lane: phi0 = 0 and
+// hp = phi).  One atomic per warp.
+template <typename R>
+__global__ void health_kernel(Layout L, const R *__restrict__ hp, const R *__restrict__ u,
+                              const R *__restrict__ v, double phi0, unsigned long long *bad) {
+  const int64_t ncell = (int64_t)L.N * L.N * 6;
+  for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x; q0 < ncell; q0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = q0 + threadIdx.x;
+    bool b = false;
+    if (q < ncell) {
+      const int i = 1 + (int)(q % L.N), j = 1 + (int)((q / L.N) % L.N), p = (int)(q / ((int64_t)L.N * L.N));
+      const int64_t c = L.idx(i, j, p);
+      const double ph = phi0 + (double)hp[c];
+      b = !(ph > 0.) || !isfinite((double)u[c]) || !isfinite((double)v[c]);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, b);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(bad, (unsigned long long)__popc(m));
+  }
+}
 
 #define CCS_TRY(h, call)                                                       \
   do {                                                                         \
@@ -85,6 +107,7 @@ struct ccs_handle {
   int64_t launches = 0;
   // diagnostics
   double *d_partials = nullptr;
+  unsigned long long *d_bad = nullptr;  // health-check counter
   // mixed lane
   struct MixedLane *mixed = nullptr;
 };
@@ -471,6 +494,7 @@ void ccs_destroy(ccs_handle *h) {
   if (h->d_stages) cudaFree(h->d_stages);
   if (h->d_work) cudaFree(h->d_work);
   if (h->d_partials) cudaFree(h->d_partials);
+  if (h->d_bad) cudaFree(h->d_bad);
   if (h->mixed) mixed_handle_destroy(h);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1008,6 +1032,29 @@ static int mixed_diag(ccs_handle *h, double *mass, double *energy) {
   if (mass) *mass = tm;
   if (energy) *energy = te;
   return CCS_OK;
+}
+
+extern "C" int ccs_check_state(ccs_handle *h, int64_t *bad_cells) {
+  if (!h) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (!h->d_bad) CCS_TRY(h, cudaMalloc(&h->d_bad, sizeof(unsigned long long)));
+  CCS_TRY(h, cudaMemsetAsync(h->d_bad, 0, sizeof(unsigned long long), h->stream));
+  const int64_t ncell = (int64_t)h->L.N * h->L.N * 6;
+  const int grid = (int)std::min<int64_t>((ncell + 255) / 256, 4096);
+  if (h->cfg.precision == CCS_MIXED) {
+    MixedLane *M = h->mixed;
+    if (!M->have_phibar) return CCS_ERR_ARG;
+    health_kernel<float><<<grid, 256, 0, h->stream>>>(h->L, M->S[0].hp, M->S[0].u, M->S[0].v, M->phibar,
+                                                       h->d_bad);
+  } else {
+    health_kernel<double><<<grid, 256, 0, h->stream>>>(h->L, h->S[0].phi, h->S[0].u, h->S[0].v, 0., h->d_bad);
+  }
+  CCS_TRY(h, cudaGetLastError());
+  unsigned long long bad = 0;
+  CCS_TRY(h, cudaMemcpyAsync(&bad, h->d_bad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  if (bad_cells) *bad_cells = (int64_t)bad;
+  return bad ? CCS_ERR_NAN : CCS_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -290,6 +290,14 @@ class Stepper:
                 "ccs_spatial_operator", self.handle)
         return tuple(t)
 
+    def check_state(self) -> int:
+        """Interior cells with non-positive depth or non-finite wind (ccs_check_state)."""
+        n = C.c_int64()
+        rc = L.lib().ccs_check_state(self.handle, C.byref(n))
+        if rc not in (L.CCS_OK, L.CCS_ERR_NAN):
+            L.check(rc, "ccs_check_state", self.handle)
+        return n.value
+
     def diag(self):
         m, e = C.c_double(), C.c_double()
         L.check(L.lib().ccs_diag(self.handle, C.byref(m), C.byref(e)), "ccs_diag", self.handle)

@@ -190,6 +190,12 @@ int ccs_get_variant(ccs_handle *h, int *variant, int *tile_x, int *tile_y);
  * entries of the outputs are set to 0).  Any output pointer may be NULL. */
 int ccs_spatial_operator(ccs_handle *h, double *tend_phiG, double *tend_u, double *tend_v);
 
+/* Health check of the current state: the number of interior cells whose depth is
+ * not positive (NaN included) or whose covariant wind is not finite, in bad_cells
+ * (may be NULL); returns CCS_ERR_NAN when there is one, CCS_OK otherwise.  The
+ * reference has no such check (a blown-up run goes on with NaNs). */
+int ccs_check_state(ccs_handle *h, int64_t *bad_cells);
+
 /* calc_total_mass / calc_total_energy (diag_mod.F90:10-53) of the current state,
  * as FP64 sums on the device. */
 int ccs_diag(ccs_handle *h, double *total_mass, double *total_energy);

@@ -124,3 +124,7 @@ def test_mixed_lane_rejects_e_reconstruction_without_device():
     rc = L.lib().ccs_init(C.byref(_cfg(precision=1, e_dissipation=1)), C.byref(mv), C.byref(h))
     assert rc == L.CCS_ERR_UNSUPPORTED
     assert not h.value
+
+
+def test_check_state_rejects_null_handle_without_device():
+    assert L.lib().ccs_check_state(None, None) == L.CCS_ERR_ARG

@@ -240,3 +240,23 @@ def test_rk3_reconstruct_halo5_60_steps_bitwise():
     m = valid_mask(mesh)
     for k in CHECK_FIELDS:
         assert bitwise_equal(g[k], o[k], m), (k, max_rel(g[k], o[k], m))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_health_check_counts_bad_cells(precision):
+    """ccs_check_state: 0 on a healthy state; planted non-finite wind and a
+    non-positive depth (host-side inputs) are counted."""
+    mesh, s, dt = seeded_case(16, 3, seed=1, oro=False)
+    kw = dict(phi_mean=8000.0 * mesh.gravity) if precision == "mixed" else {}
+    g = M.Stepper(mesh, dt, precision=precision, **kw)
+    g.set_state(s)
+    g.step(2)
+    assert g.check_state() == 0
+    bad = s.copy()
+    F = mesh.field
+    F(bad["u"])[3 + 2, 3 + 5, 1] = np.nan
+    F(bad["phi"])[3 + 7, 3 + 7, 4] = -1.0
+    F(bad["phiG"])[3 + 7, 3 + 7, 4] = -1.0
+    F(bad["phi"])[0, 5, 0] = np.nan  # a halo cell: not counted
+    g.set_state(bad)
+    assert g.check_state() == 2
