@@ -44,10 +44,20 @@ __device__ __forceinline__ double ccs_div_const(double x, double b, double y) {
   const double q0 = x * y;
   const double r = fma(-q0, b, x);
   const double q1 = fma(r, y, q0);
-  return x == 0.0 ? q0 : q1;
+  // x == +-0, tested on the bits: the FP64 pipe is the lane's bottleneck
+  return (__double_as_longlong(x) << 1) == 0 ? q0 : q1;
 }
 
 namespace {
+
+// Comparisons of non-negative doubles on the integer pipes: for +0 and positive
+// finite or infinite values the IEEE order is the order of the bit patterns read
+// as signed integers, so these give the FP64 comparisons' results without issuing
+// on the FP64 pipe (GB300 runs FP64 at 1/64 of the FP32 rate).  |x| is the bit
+// pattern with the sign cleared.
+__device__ __forceinline__ long long abs_bits(double x) {
+  return __double_as_longlong(x) & 0x7fffffffffffffffLL;
+}
 
 // WENO_limiter, spatial_operators_mod.F90:282-361.
 template <int DIR>
@@ -80,16 +90,16 @@ __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double
   const double be0 = ccs_div_const(a0 * a0 * 13., 12., y12) + b0 * b0 * 0.25;
   const double be1 = ccs_div_const(a1 * a1 * 13., 12., y12) + b1 * b1 * 0.25;
   const double be2 = ccs_div_const(a2 * a2 * 13., 12., y12) + b2 * b2 * 0.25;
-  const double tau40 = fabs(be0 - be1);
-  const double tau41 = fabs(be1 - be2);
+  // the betas are sums of squares (never -0 or negative), the taus absolute values
+  const long long t40 = abs_bits(be0 - be1), t41 = abs_bits(be1 - be2);
   const double tau5 = fabs(be2 - be0);
-  double mn = be0;
-  if (be1 < mn) mn = be1;
-  if (be2 < mn) mn = be2;
+  long long mn = __double_as_longlong(be0);
+  if (__double_as_longlong(be1) < mn) mn = __double_as_longlong(be1);
+  if (__double_as_longlong(be2) < mn) mn = __double_as_longlong(be2);
   double w0, w1, w2;
-  if (tau40 <= mn && tau41 > mn) {
+  if (t40 <= mn && t41 > mn) {
     w0 = 1. / 3.; w1 = 2. / 3.; w2 = 0.;
-  } else if (tau40 > mn && tau41 < mn) {
+  } else if (t40 > mn && t41 < mn) {
     w0 = 0.; w1 = 2. / 3.; w2 = 1. / 3.;
   } else {
     const double eps = 1.E-2;
@@ -233,8 +243,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
       const double phitBdy = 0.5 * (pa + pb);
       const double e1 = uBdy - sqrt(0.5 * (ga + gb) * phitBdy);
       const double e2 = uBdy + sqrt(0.5 * (ga + gb) * phitBdy);
-      double mx = fabs(e1);
-      if (fabs(e2) > mx) mx = fabs(e2);
+      const double mx = abs_bits(e2) > abs_bits(e1) ? fabs(e2) : fabs(e1);
       rec[0 * NF + face] = 0.5 * (Fp + Fn - mx * (Pn - Pp));
       rec[1 * NF + face] = 0.5 * (Ep + En - mx * (dn - dp));
     }
