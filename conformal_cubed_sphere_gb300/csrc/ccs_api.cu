@@ -98,6 +98,7 @@ struct ccs_handle {
   int nwork = 0;
   int grid = 0;
   int var = 0;  // tile variant of the FP64 stage kernel (kF64Tiles)
+  int op = CCS_OP_WENO;  // spatial operator (ccs_set_operator)
   bool sphere_valid = false;
   cudaGraphExec_t g_step = nullptr, g_step_sw = nullptr;
   // timing
@@ -161,6 +162,8 @@ static void mixed_handle_destroy(ccs_handle *h);
 static int mixed_set_state(ccs_handle *h, const ccs_state_view *s, bool sync);
 static int mixed_get_state(ccs_handle *h, ccs_state_view *s, bool sync);
 static int mixed_sync(ccs_handle *h);
+static int mixed_build_stages(ccs_handle *h);
+static bool mixed_has_stages(const ccs_handle *h);
 static int mixed_step(ccs_handle *h, int nsteps, bool sync);
 static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv);
 static int mixed_diag(ccs_handle *h, double *mass, double *energy);
@@ -269,6 +272,7 @@ static int build_f64_lane(ccs_handle *h) {
   base.dx = c.dx; base.dy = c.dy;
   base.dx60 = 60. * c.dx; base.dy60 = 60. * c.dy;
   base.ediss = c.e_dissipation;
+  base.op = h->op;
   auto mk = [&](int kind, int in, int out, double c1) {
     F64Stage s = base;
     s.kind = kind;
@@ -581,8 +585,12 @@ int ccs_set_operator(ccs_handle *h, int op) {
   if (!h) return CCS_ERR_ARG;
   if (op != CCS_OP_WENO && op != CCS_OP_CENTRAL2 && op != CCS_OP_CENTRAL4 && op != CCS_OP_CENTRAL6)
     return CCS_ERR_ARG;
-  if (h->cfg.precision == CCS_MIXED) return op == CCS_OP_WENO ? CCS_OK : CCS_ERR_UNSUPPORTED;
   cudaSetDevice(h->cfg.device);
+  h->op = op;
+  if (h->cfg.precision == CCS_MIXED) {
+    // the stage descriptors exist once the state (and with it phibar) is set
+    return mixed_has_stages(h) ? mixed_build_stages(h) : CCS_OK;
+  }
   for (F64Stage &s : h->h_stages) s.op = op;
   // the captured graphs read the descriptors from device memory: updating them in
   // place (after the stream's pending steps) is all a change needs
@@ -827,6 +835,12 @@ static int mixed_build_stages(ccs_handle *h) {
   base.eps_F = (float)(1.e-2 / (a2 * a2));
   base.eps_P = (float)(1.e-2 / (a2 * a2));
   base.ediss = c.e_dissipation;
+  base.op = h->op;
+  {
+    const double den = h->op == CCS_OP_CENTRAL2 ? 2. : h->op == CCS_OP_CENTRAL4 ? 12. : 60.;
+    base.rdxc = (float)(1. / (den * c.dx));
+    base.rdyc = (float)(1. / (den * c.dy));
+  }
   auto mk = [&](int kind, int in, int out, double c1) {
     MixedStage s = base;
     s.kind = kind;
@@ -943,6 +957,8 @@ static int mixed_get_state(ccs_handle *h, ccs_state_view *s, bool sync) {
   if (sync) CCS_TRY(h, cudaStreamSynchronize(M->cout));
   return CCS_OK;
 }
+
+static bool mixed_has_stages(const ccs_handle *h) { return h->mixed->have_phibar; }
 
 static int mixed_sync(ccs_handle *h) {
   MixedLane *M = h->mixed;

@@ -57,6 +57,8 @@ struct MixedStage {
   float eps_F;  // eps of the flux / a^2 (1e-2 / a^4)
   float eps_P;  // eps of phitG / a^2 (1e-2 / a^4)
   int kind, ediss;
+  int op;             // CCS_OP_WENO, or the central-difference order 2 / 4 / 6
+  float rdxc, rdyc;   // 1 / (2 dx), 1 / (12 dx) or 1 / (60 dx) for the central operator
 };
 
 // Kernel variants: the tile shape (cells per work item) of each lane's stage kernel.

@@ -170,6 +170,18 @@ __device__ __forceinline__ float diff6(const float *f, int s) {
   return t + f[3 * s];
 }
 
+// The numerator of the centred difference of order op (2, 4, 6) of f[-3s .. 3s]
+// around f[0] (spatial_operators_mod_2nd.F90:54-59, _4th.F90:58-63, _6th.F90:62-67);
+// the caller multiplies by 1 / (2 dx), 1 / (12 dx) or 1 / (60 dx).
+__device__ __forceinline__ float central(int op, const float *f, int s) {
+  if (op == 2) return f[s] - f[-s];
+  if (op == 4) {
+    const float t = fmaf(-8.f, f[-s], f[-2 * s]);
+    return fmaf(8.f, f[s], t) - f[2 * s];
+  }
+  return diff6(f, s);
+}
+
 template <class T>
 struct SmemMx {
   MixedStage st;  // this work item's stage descriptor
@@ -337,7 +349,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     __syncthreads();
 
     // ---- phase 2: lines -> face values (warps 0-3 rows, 4-7 columns) ---------
-    {
+    if (st.op == CCS_OP_WENO) {  // (the central-difference operators have no faces)
       // segment seg of a line covers faces 0-8 (seg 0) or 8 seg + 1 .. 8 seg + 8
       if (tid < 4 * TY) {
         const int line = tid % TY, seg = tid / TY;
@@ -383,13 +395,23 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       const int i = i0 + li, j = j0 + lj;
       if (i > N || j > N) continue;
       const int r = (lj + 3) * SP + li + 3;
-      const float divx = (S.gx[0][lj][li + 1] - S.gx[0][lj][li] + (S.F[r] - S.F[r - 1])) * st.rdx;
-      const float dEdx = (S.gx[1][lj][li + 1] - S.gx[1][lj][li] + (S.E[r] - S.E[r - 1])) * st.rdx;
-      const float divy = (S.gy[0][lj + 1][li] - S.gy[0][lj][li] + (S.G[r] - S.G[r - SP])) * st.rdy;
-      const float dEdy = (S.gy[1][lj + 1][li] - S.gy[1][lj][li] + (S.E[r] - S.E[r - SP])) * st.rdy;
-      const float *vv = S.v + r, *uu = S.u + r;
-      const float dvdx = diff6(vv, 1) * st.rdx60;
-      const float dudy = diff6(uu, SP) * st.rdy60;
+      float divx, dEdx, divy, dEdy, dvdx, dudy;
+      if (st.op == CCS_OP_WENO) {
+        divx = (S.gx[0][lj][li + 1] - S.gx[0][lj][li] + (S.F[r] - S.F[r - 1])) * st.rdx;
+        dEdx = (S.gx[1][lj][li + 1] - S.gx[1][lj][li] + (S.E[r] - S.E[r - 1])) * st.rdx;
+        divy = (S.gy[0][lj + 1][li] - S.gy[0][lj][li] + (S.G[r] - S.G[r - SP])) * st.rdy;
+        dEdy = (S.gy[1][lj + 1][li] - S.gy[1][lj][li] + (S.E[r] - S.E[r - SP])) * st.rdy;
+        dvdx = diff6(S.v + r, 1) * st.rdx60;
+        dudy = diff6(S.u + r, SP) * st.rdy60;
+      } else {  // spatial_operators_mod_{2nd,4th,6th}.F90: centred differences of the cell values
+        const int op = st.op;
+        divx = central(op, S.F + r, 1) * st.rdxc;
+        dEdx = central(op, S.E + r, 1) * st.rdxc;
+        dvdx = central(op, S.v + r, 1) * st.rdxc;
+        divy = central(op, S.G + r, SP) * st.rdyc;
+        dEdy = central(op, S.E + r, SP) * st.rdyc;
+        dudy = central(op, S.u + r, SP) * st.rdyc;
+      }
       const int64_t c = L.idx(i, j, p);
       const float vort = dvdx - dudy + q_fs[k];
       const float tp = -(divx + divy) * q_is[k];

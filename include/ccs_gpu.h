@@ -163,9 +163,9 @@ int ccs_get_state_async(ccs_handle *h, ccs_state_view *s);
 
 /* Selects the spatial operator of the handle's steps (default CCS_OP_WENO): the
  * choice the reference makes at build time by compiling one of its four
- * spatial_operators_mod sources.  FP64 lane only (CCS_ERR_UNSUPPORTED on the mixed
- * lane for anything but CCS_OP_WENO); a batch copies its members' operators when
- * it is created.  No counterpart call in the reference. */
+ * spatial_operators_mod sources.  Both lanes (the FP64 lane operation for
+ * operation, the mixed lane in FP32 like its WENO operator); a batch copies its
+ * members' operators when it is created.  No counterpart call in the reference. */
 int ccs_set_operator(ccs_handle *h, int op);
 
 /* ---- kernel variants and the autotuner (no counterpart in the reference) ----
