@@ -19,7 +19,9 @@ from . import _lib as L
 PI = np.pi
 D2R = PI / 180.0
 
-# BASELINE constants (the reference hard-codes radius 6371229 in constants_mod.F90:9)
+# planet constants of the benchmark cases: a = 6.371e6 m (the reference's
+# constants_mod.F90:9 has 6371229 m; Mesh(radius=...) takes either), g and Omega as
+# constants_mod.F90:6,12
 RADIUS = 6.371e6
 GRAVITY = 9.80616
 OMEGA = 7.292e-5
