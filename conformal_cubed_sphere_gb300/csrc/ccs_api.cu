@@ -971,7 +971,8 @@ static int mixed_enqueue_step(ccs_handle *h) {
   MixedLane *M = h->mixed;
   for (int k = 0; k < M->n_rk; k++) {
     if (h->timing) CCS_TRY(h, cudaEventRecord(h->ev0, h->stream));
-    CCS_TRY(h, launch_mixed_stage(M->var, M->d_stages + k, M->d_work, M->nwork, M->grid, h->stream));
+    CCS_TRY(h, launch_mixed_stage(M->var, h->op != CCS_OP_WENO, M->d_stages + k, M->d_work, M->nwork, M->grid,
+                                  h->stream));
     if (h->timing) {
       CCS_TRY(h, cudaEventRecord(h->ev1, h->stream));
       CCS_TRY(h, cudaEventSynchronize(h->ev1));
@@ -1016,7 +1017,8 @@ static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv) {
   if (!M->have_phibar) return CCS_ERR_ARG;
   const Layout &L = h->L;
   const size_t nref = (size_t)L.nh * L.nh * 6;
-  CCS_TRY(h, launch_mixed_stage(M->var, M->d_stages + M->n_rk, M->d_work, M->nwork, M->grid, h->stream));
+  CCS_TRY(h, launch_mixed_stage(M->var, h->op != CCS_OP_WENO, M->d_stages + M->n_rk, M->d_work, M->nwork,
+                                M->grid, h->stream));
   const double a2 = h->cfg.radius * h->cfg.radius;
   CCS_TRY(h, cudaStreamSynchronize(M->cout));  // no copy may still read the out slots
   double *o = M->stage_out[0];
@@ -1126,7 +1128,8 @@ static int time_stages(ccs_handle *h, int reps, double *us) {
   auto launch = [&](int k) -> cudaError_t {
     if (mx) {
       MixedLane *M = h->mixed;
-      return launch_mixed_stage(M->var, M->d_stages + k, M->d_work, M->nwork, M->grid, h->stream);
+      return launch_mixed_stage(M->var, h->op != CCS_OP_WENO, M->d_stages + k, M->d_work, M->nwork, M->grid,
+                                h->stream);
     }
     return launch_f64_stage(h->var, h->d_stages + k, h->d_work, h->nwork, h->grid, h->stream);
   };
@@ -1205,6 +1208,7 @@ extern "C" int ccs_autotune(ccs_handle *h, int reps, int force, int *chosen, dou
 // ---------------------------------------------------------------------------
 struct BatchGroup {
   int lane = 0, n_rk = 0, nmem = 0, var = 0;
+  bool central = false;  // the members' spatial operator is a central difference
   std::vector<ccs_handle *> members;
   void *d_stages = nullptr;  // [n_rk + 1][nmem] F64Stage or MixedStage (last row: F64 final with sphere winds)
   WorkItem *d_work = nullptr;
@@ -1237,7 +1241,7 @@ static int batch_enqueue(ccs_batch *b, bool with_sw) {
         e = launch_f64_stage(g.var, (const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork,
                              g.grid, g.stream);
       } else {
-        e = launch_mixed_stage(g.var, (const MixedStage *)g.d_stages + (size_t)k * g.nmem, g.d_work, g.nwork,
+        e = launch_mixed_stage(g.var, g.central, (const MixedStage *)g.d_stages + (size_t)k * g.nmem, g.d_work, g.nwork,
                                g.grid, g.stream);
       }
       if (e != cudaSuccess) {
@@ -1269,12 +1273,15 @@ extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **o
   auto member_var = [](const ccs_handle *m) { return m->cfg.precision == CCS_MIXED ? m->mixed->var : m->var; };
   for (int lane = 0; lane < 2; lane++)
     for (int scheme = 0; scheme < 2; scheme++)
-      for (int var = 0; var < (lane == CCS_FP64 ? F64_NVAR : MX_NVAR); var++) {
+      for (int var = 0; var < (lane == CCS_FP64 ? F64_NVAR : MX_NVAR); var++)
+        for (int central = 0; central < 2; central++) {
       BatchGroup g;
       g.lane = lane;
       g.var = var;
+      g.central = central != 0;
       for (int k = 0; k < n; k++)
-        if (members[k]->cfg.precision == lane && members[k]->cfg.scheme == scheme && member_var(members[k]) == var)
+        if (members[k]->cfg.precision == lane && members[k]->cfg.scheme == scheme &&
+            member_var(members[k]) == var && (members[k]->op != CCS_OP_WENO) == g.central)
           g.members.push_back(members[k]);
       if (g.members.empty()) continue;
       g.nmem = (int)g.members.size();

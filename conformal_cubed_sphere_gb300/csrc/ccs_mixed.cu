@@ -293,7 +293,8 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
 #endif
 constexpr int kP1Unroll = CCS_MIXED_P1_UNROLL;
 
-template <class T>
+// CENTRAL: the central-difference operators (no face phases); else WENO-Z.
+template <class T, bool CENTRAL>
 __global__ void __launch_bounds__(T::NT, CCS_MIXED_MIN_CTAS * 32 / T::TY)
 mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
   constexpr int TX = T::TX, TY = T::TY, NT = T::NT, RX = T::RX, RY = T::RY;
@@ -349,7 +350,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     __syncthreads();
 
     // ---- phase 2: lines -> face values (warps 0-3 rows, 4-7 columns) ---------
-    if (st.op == CCS_OP_WENO) {  // (the central-difference operators have no faces)
+    if (!CENTRAL) {  // (the central-difference operators have no faces)
       // segment seg of a line covers faces 0-8 (seg 0) or 8 seg + 1 .. 8 seg + 8
       if (tid < 4 * TY) {
         const int line = tid % TY, seg = tid / TY;
@@ -396,7 +397,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       if (i > N || j > N) continue;
       const int r = (lj + 3) * SP + li + 3;
       float divx, dEdx, divy, dEdy, dvdx, dudy;
-      if (st.op == CCS_OP_WENO) {
+      if (!CENTRAL) {
         divx = (S.gx[0][lj][li + 1] - S.gx[0][lj][li] + (S.F[r] - S.F[r - 1])) * st.rdx;
         dEdx = (S.gx[1][lj][li + 1] - S.gx[1][lj][li] + (S.E[r] - S.E[r - 1])) * st.rdx;
         divy = (S.gy[0][lj + 1][li] - S.gy[0][lj][li] + (S.G[r] - S.G[r - SP])) * st.rdy;
@@ -651,27 +652,27 @@ static_assert(MxT0::TX == kMxTiles[0].tx && MxT0::TY == kMxTiles[0].ty, "tile ta
 static_assert(MxT1::TX == kMxTiles[1].tx && MxT1::TY == kMxTiles[1].ty, "tile table");
 
 template <class T>
-int mx_grid_for(int device) {
+int mx_grid_for(int device) {  // the WENO instance bounds the occupancy of both
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   constexpr int smem = (int)sizeof(SmemMx<T>);
-  cudaFuncSetAttribute(mixed_stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel<T>, T::NT, smem);
+  cudaFuncSetAttribute(mixed_stage_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel<T, false>, T::NT, smem);
   if (per < 1) per = 1;
   return sms * per;
 }
 
-template <class T>
+template <class T, bool CENTRAL>
 cudaError_t mx_launch(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
   constexpr int smem = (int)sizeof(SmemMx<T>);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(mixed_stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(mixed_stage_kernel<T, CENTRAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr_set = true;
   }
   if (grid > nwork) grid = nwork;
   if (grid < 1) return cudaSuccess;
-  mixed_stage_kernel<T><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
+  mixed_stage_kernel<T, CENTRAL><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
   return cudaGetLastError();
 }
 
@@ -681,10 +682,13 @@ int mixed_max_grid(int var, int device) {
   return var == 1 ? mx_grid_for<MxT1>(device) : mx_grid_for<MxT0>(device);
 }
 
-cudaError_t launch_mixed_stage(int var, const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid,
-                               cudaStream_t s) {
-  return var == 1 ? mx_launch<MxT1>(d_stages, d_work, nwork, grid, s)
-                  : mx_launch<MxT0>(d_stages, d_work, nwork, grid, s);
+cudaError_t launch_mixed_stage(int var, bool central, const MixedStage *d_stages, const WorkItem *d_work,
+                               int nwork, int grid, cudaStream_t s) {
+  if (central)
+    return var == 1 ? mx_launch<MxT1, true>(d_stages, d_work, nwork, grid, s)
+                    : mx_launch<MxT0, true>(d_stages, d_work, nwork, grid, s);
+  return var == 1 ? mx_launch<MxT1, false>(d_stages, d_work, nwork, grid, s)
+                  : mx_launch<MxT0, false>(d_stages, d_work, nwork, grid, s);
 }
 
 static int ew_grid(const Layout &L) {

@@ -99,3 +99,24 @@ def test_batch_groups_members_by_variant():
         m = valid_mask(mesh)
         for k in CHECK_FIELDS:
             assert bitwise_equal(a[k], b[k], m), k
+
+
+def test_batch_groups_mixed_members_by_operator():
+    """Mixed members with the WENO and a central operator run in separate launches
+    of one batch and equal their single runs bit for bit."""
+    mesh, s, dt = seeded_case(24, 3, seed=21, oro=True)
+    kw = dict(phi_mean=8000.0 * mesh.gravity)
+    members = []
+    for op in (L.CCS_OP_WENO, L.CCS_OP_CENTRAL4, L.CCS_OP_CENTRAL6):
+        x = M.Stepper(mesh, 0.5 * dt, precision="mixed", operator=op, **kw)
+        x.set_state(s)
+        members.append((op, x))
+    M.Batch([x for _, x in members]).step(3)
+    m = valid_mask(mesh)
+    for op, x in members:
+        r = M.Stepper(mesh, 0.5 * dt, precision="mixed", operator=op, **kw)
+        r.set_state(s)
+        r.step(3)
+        a, b = x.get_state(), r.get_state()
+        for k in CHECK_FIELDS:
+            assert bitwise_equal(a[k], b[k], m), (op, k)
