@@ -137,8 +137,6 @@ static int validate_config(const ccs_config *c) {
   if (c->scheme != CCS_RK4 && c->scheme != CCS_RK3_TVD) return CCS_ERR_ARG;
   if (c->precision != CCS_FP64 && c->precision != CCS_MIXED) return CCS_ERR_ARG;
   if (c->e_dissipation != CCS_EDISS_ZERO && c->e_dissipation != CCS_EDISS_RECONSTRUCT) return CCS_ERR_ARG;
-  // the mixed lane implements the reference's data flow only (never-written face slots read as 0)
-  if (c->precision == CCS_MIXED && c->e_dissipation != CCS_EDISS_ZERO) return CCS_ERR_UNSUPPORTED;
   if (!(c->dx > 0.) || !(c->dy > 0.) || !(c->dt > 0.) || !(c->radius > 0.) || !(c->gravity > 0.))
     return CCS_ERR_ARG;
   if (!std::isfinite(c->dx) || !std::isfinite(c->dy) || !std::isfinite(c->dt) || !std::isfinite(c->omega))
@@ -960,6 +958,14 @@ static int mixed_get_state(ccs_handle *h, ccs_state_view *s, bool sync) {
 
 static bool mixed_has_stages(const ccs_handle *h) { return h->mixed->have_phibar; }
 
+// one launch of the handle's mixed stage kernel instance (tile variant, operator
+// family, E-flux option) over stage descriptor d
+static cudaError_t mixed_launch(ccs_handle *h, const MixedStage *d) {
+  MixedLane *M = h->mixed;
+  return launch_mixed_stage(M->var, h->op != CCS_OP_WENO, h->cfg.e_dissipation != CCS_EDISS_ZERO, d, M->d_work,
+                            M->nwork, M->grid, h->stream);
+}
+
 static int mixed_sync(ccs_handle *h) {
   MixedLane *M = h->mixed;
   CCS_TRY(h, cudaStreamSynchronize(M->cin));
@@ -971,8 +977,7 @@ static int mixed_enqueue_step(ccs_handle *h) {
   MixedLane *M = h->mixed;
   for (int k = 0; k < M->n_rk; k++) {
     if (h->timing) CCS_TRY(h, cudaEventRecord(h->ev0, h->stream));
-    CCS_TRY(h, launch_mixed_stage(M->var, h->op != CCS_OP_WENO, M->d_stages + k, M->d_work, M->nwork, M->grid,
-                                  h->stream));
+    CCS_TRY(h, mixed_launch(h, M->d_stages + k));
     if (h->timing) {
       CCS_TRY(h, cudaEventRecord(h->ev1, h->stream));
       CCS_TRY(h, cudaEventSynchronize(h->ev1));
@@ -1017,8 +1022,7 @@ static int mixed_tend(ccs_handle *h, double *tp, double *tu, double *tv) {
   if (!M->have_phibar) return CCS_ERR_ARG;
   const Layout &L = h->L;
   const size_t nref = (size_t)L.nh * L.nh * 6;
-  CCS_TRY(h, launch_mixed_stage(M->var, h->op != CCS_OP_WENO, M->d_stages + M->n_rk, M->d_work, M->nwork,
-                                M->grid, h->stream));
+  CCS_TRY(h, mixed_launch(h, M->d_stages + M->n_rk));
   const double a2 = h->cfg.radius * h->cfg.radius;
   CCS_TRY(h, cudaStreamSynchronize(M->cout));  // no copy may still read the out slots
   double *o = M->stage_out[0];
@@ -1128,8 +1132,7 @@ static int time_stages(ccs_handle *h, int reps, double *us) {
   auto launch = [&](int k) -> cudaError_t {
     if (mx) {
       MixedLane *M = h->mixed;
-      return launch_mixed_stage(M->var, h->op != CCS_OP_WENO, M->d_stages + k, M->d_work, M->nwork, M->grid,
-                                h->stream);
+      return mixed_launch(h, M->d_stages + k);
     }
     return launch_f64_stage(h->var, h->d_stages + k, h->d_work, h->nwork, h->grid, h->stream);
   };
@@ -1209,6 +1212,7 @@ extern "C" int ccs_autotune(ccs_handle *h, int reps, int force, int *chosen, dou
 struct BatchGroup {
   int lane = 0, n_rk = 0, nmem = 0, var = 0;
   bool central = false;  // the members' spatial operator is a central difference
+  bool ediss = false;    // the members reconstruct the E-flux dissipation
   std::vector<ccs_handle *> members;
   void *d_stages = nullptr;  // [n_rk + 1][nmem] F64Stage or MixedStage (last row: F64 final with sphere winds)
   WorkItem *d_work = nullptr;
@@ -1241,7 +1245,8 @@ static int batch_enqueue(ccs_batch *b, bool with_sw) {
         e = launch_f64_stage(g.var, (const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork,
                              g.grid, g.stream);
       } else {
-        e = launch_mixed_stage(g.var, g.central, (const MixedStage *)g.d_stages + (size_t)k * g.nmem, g.d_work, g.nwork,
+        e = launch_mixed_stage(g.var, g.central, g.ediss, (const MixedStage *)g.d_stages + (size_t)k * g.nmem,
+                               g.d_work, g.nwork,
                                g.grid, g.stream);
       }
       if (e != cudaSuccess) {
@@ -1274,14 +1279,17 @@ extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **o
   for (int lane = 0; lane < 2; lane++)
     for (int scheme = 0; scheme < 2; scheme++)
       for (int var = 0; var < (lane == CCS_FP64 ? F64_NVAR : MX_NVAR); var++)
-        for (int central = 0; central < 2; central++) {
+        for (int central = 0; central < 2; central++)
+          for (int ediss = 0; ediss < 2; ediss++) {
       BatchGroup g;
       g.lane = lane;
       g.var = var;
       g.central = central != 0;
+      g.ediss = ediss != 0;
       for (int k = 0; k < n; k++)
         if (members[k]->cfg.precision == lane && members[k]->cfg.scheme == scheme &&
-            member_var(members[k]) == var && (members[k]->op != CCS_OP_WENO) == g.central)
+            member_var(members[k]) == var && (members[k]->op != CCS_OP_WENO) == g.central &&
+            (members[k]->cfg.e_dissipation != CCS_EDISS_ZERO) == g.ediss)
           g.members.push_back(members[k]);
       if (g.members.empty()) continue;
       g.nmem = (int)g.members.size();

@@ -76,9 +76,10 @@ cudaError_t launch_f64_stage(int var, const F64Stage *d_stages, const WorkItem *
                              cudaStream_t s);
 int f64_max_grid(int var, int device);
 
-// central: every stage in d_stages uses a central-difference operator (else WENO-Z)
-cudaError_t launch_mixed_stage(int var, bool central, const MixedStage *d_stages, const WorkItem *d_work,
-                               int nwork, int grid, cudaStream_t s);
+// central: every stage in d_stages uses a central-difference operator (else WENO-Z);
+// ediss: every stage reconstructs the E-flux dissipation (CCS_EDISS_RECONSTRUCT)
+cudaError_t launch_mixed_stage(int var, bool central, bool ediss, const MixedStage *d_stages,
+                               const WorkItem *d_work, int nwork, int grid, cudaStream_t s);
 int mixed_max_grid(int var, int device);
 cudaError_t launch_mixed_import(const Layout &L, const double *phi, const double *u, const double *v,
                                 double phibar, double inv_a2, StateMixed out, float *lohp, float *lou,

@@ -197,13 +197,17 @@ __device__ __forceinline__ bool corner(int i, int j, int N) { return (i < 1 || i
 // the cells' difference windows slide along the line so that each cell costs one
 // new shared-memory value per field; the face between two cells is formed from
 // the left cell's "+" and the right cell's "-" corrections in registers.
-template <bool XDIR, class T>
+// EDISS: the E flux gets the Rusanov dissipation of the covariant wind along the
+// line (u at x-faces, v at y-faces: CCS_EDISS_RECONSTRUCT), reconstructed like the
+// other fields and paired with E in f32x2; its eps scales like the flux's (1e-2 / a^4).
+template <bool XDIR, bool EDISS, class T>
 __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict__ Qflux,
                                           const float *__restrict__ cvel, const float *__restrict__ lam,
                                           const Layout &L, int line, int f0,
                                           int NFACE, int startg, int lineg) {
   const MixedStage &st = S.st;
   const float phibar = st.phibar, epsF = 4.f * st.eps_F, epsE = 4.f * st.eps_E, epsP = 4.f * st.eps_P;
+  const float *__restrict__ Uw = XDIR ? S.u : S.v;  // the wind component along the line
   const int stp = XDIR ? 1 : SP;
   const int base = XDIR ? (line + 3) * SP + 2 : 2 * SP + line + 3;  // cell ci = 0 of the line
   int o = base + (f0 - 2) * stp;
@@ -225,6 +229,11 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
   float Flast = Fv[3], Elast = Ev[3], slast = sv[3], qlast = q3;
   float hc = hv[2], hc1 = hv[3];  // hs at c and c+1
   float pDFp = 0.f, pDEp = 0.f, pDPp = 0.f, pU = 0.f, pH = 0.f;
+  float dU0 = 0.f, dU1 = 0.f, dU2 = 0.f, Ulast = 0.f, pDUp = 0.f;
+  if constexpr (EDISS) {
+    const float u0 = Uw[o], u1 = Uw[o + stp], u2 = Uw[o + 2 * stp], u3 = Uw[o + 3 * stp];
+    dU0 = u1 - u0; dU1 = u2 - u1; dU2 = u3 - u2; Ulast = u3;
+  }
   // face wave-speed metric, fetched one face ahead of its use by walking a pointer
   // along the line; faces of a partial tile beyond N are read (and not used) from
   // the 32 padding rows the metric arrays carry after each panel block
@@ -254,7 +263,17 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
       DFp = Dp2.x; DPp = Dp2.y; DFm = Dm2.x; DPm = Dm2.y;
     }
 #endif
-    weno_d(dE0, dE1, dE2, dE3, epsE, DEp, DEm);
+    float DUp = 0.f, DUm = 0.f, Un = 0.f, dU3 = 0.f;
+    if constexpr (EDISS) {
+      Un = Uw[on];
+      dU3 = Un - Ulast;
+      float2 Dp2, Dm2;
+      weno_d2(make_float2(dE0, dU0), make_float2(dE1, dU1), make_float2(dE2, dU2), make_float2(dE3, dU3),
+              make_float2(epsE, epsF), Dp2, Dm2);
+      DEp = Dp2.x; DUp = Dp2.y; DEm = Dm2.x; DUm = Dm2.y;
+    } else {
+      weno_d(dE0, dE1, dE2, dE3, epsE, DEp, DEm);
+    }
     const float uc = cvel[base + ci * stp];
     if (k > 0) {
       const int fi = ci - 1;         // face between line cells ci-1 and ci
@@ -264,7 +283,8 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
         const float pB = fmaf(0.5f, pH + hc, phibar);
         const float lm = fabsf(uB) + sqrt_approx(fmaxf(lam_cur * pB, 0.f));
         const float gF = 0.5f * fmaf(-lm, dP1 + DPm - pDPp, dF1 + pDFp + DFm);
-        const float gE = 0.5f * (dE1 + pDEp + DEm);
+        const float gE = EDISS ? 0.5f * fmaf(-lm, dU1 + DUm - pDUp, dE1 + pDEp + DEm)
+                               : 0.5f * (dE1 + pDEp + DEm);
         if (XDIR) {
           S.gx[0][line][fi] = gF;
           S.gx[1][line][fi] = gE;
@@ -280,6 +300,11 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
     dP0 = dP1; dP1 = dP2; dP2 = dP3;
     Flast = Fn; Elast = En; slast = sn; qlast = qn;
     hc = hc1; hc1 = hn;
+    if constexpr (EDISS) {
+      pDUp = DUp;
+      dU0 = dU1; dU1 = dU2; dU2 = dU3;
+      Ulast = Un;
+    }
   }
 }
 
@@ -294,7 +319,7 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
 constexpr int kP1Unroll = CCS_MIXED_P1_UNROLL;
 
 // CENTRAL: the central-difference operators (no face phases); else WENO-Z.
-template <class T, bool CENTRAL>
+template <class T, bool CENTRAL, bool EDISS>
 __global__ void __launch_bounds__(T::NT, CCS_MIXED_MIN_CTAS * 32 / T::TY)
 mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
   constexpr int TX = T::TX, TY = T::TY, NT = T::NT, RX = T::RX, RY = T::RY;
@@ -355,11 +380,11 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       if (tid < 4 * TY) {
         const int line = tid % TY, seg = tid / TY;
         const int f0 = seg == 0 ? 0 : 1 + 8 * seg, nface = seg == 0 ? 9 : 8;
-        if (j0 + line <= N) tile_line<true>(S, S.F, S.uC, st.m.lamx, L, line, f0, nface, i0 - 1, j0 + line);
+        if (j0 + line <= N) tile_line<true, EDISS>(S, S.F, S.uC, st.m.lamx, L, line, f0, nface, i0 - 1, j0 + line);
       } else {
         const int t = tid - 4 * TY, line = t % TX, seg = t / TX;
         const int f0 = seg == 0 ? 0 : 1 + 8 * seg, nface = seg == 0 ? 9 : 8;
-        if (i0 + line <= N) tile_line<false>(S, S.G, S.vC, st.m.lamy, L, line, f0, nface, j0 - 1, i0 + line);
+        if (i0 + line <= N) tile_line<false, EDISS>(S, S.G, S.vC, st.m.lamy, L, line, f0, nface, j0 - 1, i0 + line);
       }
     }
     // Global operands of phase 3 for this thread's four cells, loaded before the
@@ -652,28 +677,37 @@ static_assert(MxT0::TX == kMxTiles[0].tx && MxT0::TY == kMxTiles[0].ty, "tile ta
 static_assert(MxT1::TX == kMxTiles[1].tx && MxT1::TY == kMxTiles[1].ty, "tile table");
 
 template <class T>
-int mx_grid_for(int device) {  // the WENO instance bounds the occupancy of both
+int mx_grid_for(int device) {  // the WENO instance bounds the occupancy of all
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   constexpr int smem = (int)sizeof(SmemMx<T>);
-  cudaFuncSetAttribute(mixed_stage_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel<T, false>, T::NT, smem);
+  cudaFuncSetAttribute(mixed_stage_kernel<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel<T, false, false>, T::NT, smem);
   if (per < 1) per = 1;
   return sms * per;
 }
 
-template <class T, bool CENTRAL>
+template <class T, bool CENTRAL, bool EDISS>
 cudaError_t mx_launch(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
   constexpr int smem = (int)sizeof(SmemMx<T>);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(mixed_stage_kernel<T, CENTRAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(mixed_stage_kernel<T, CENTRAL, EDISS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         smem);
     attr_set = true;
   }
   if (grid > nwork) grid = nwork;
   if (grid < 1) return cudaSuccess;
-  mixed_stage_kernel<T, CENTRAL><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
+  mixed_stage_kernel<T, CENTRAL, EDISS><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
   return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t mx_launch_any(bool central, bool ediss, const MixedStage *d_stages, const WorkItem *d_work, int nwork,
+                          int grid, cudaStream_t s) {
+  if (central) return mx_launch<T, true, false>(d_stages, d_work, nwork, grid, s);  // no faces: no E term
+  if (ediss) return mx_launch<T, false, true>(d_stages, d_work, nwork, grid, s);
+  return mx_launch<T, false, false>(d_stages, d_work, nwork, grid, s);
 }
 
 }  // namespace
@@ -682,13 +716,10 @@ int mixed_max_grid(int var, int device) {
   return var == 1 ? mx_grid_for<MxT1>(device) : mx_grid_for<MxT0>(device);
 }
 
-cudaError_t launch_mixed_stage(int var, bool central, const MixedStage *d_stages, const WorkItem *d_work,
-                               int nwork, int grid, cudaStream_t s) {
-  if (central)
-    return var == 1 ? mx_launch<MxT1, true>(d_stages, d_work, nwork, grid, s)
-                    : mx_launch<MxT0, true>(d_stages, d_work, nwork, grid, s);
-  return var == 1 ? mx_launch<MxT1, false>(d_stages, d_work, nwork, grid, s)
-                  : mx_launch<MxT0, false>(d_stages, d_work, nwork, grid, s);
+cudaError_t launch_mixed_stage(int var, bool central, bool ediss, const MixedStage *d_stages,
+                               const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
+  return var == 1 ? mx_launch_any<MxT1>(central, ediss, d_stages, d_work, nwork, grid, s)
+                  : mx_launch_any<MxT0>(central, ediss, d_stages, d_work, nwork, grid, s);
 }
 
 static int ew_grid(const Layout &L) {

@@ -62,7 +62,7 @@ enum {
  * y-faces, v only at x-faces).  ZERO reads them as 0.0, i.e. E at a face is the
  * plain average of its two reconstructions (what a freshly zeroed scratch gives).
  * RECONSTRUCT fills them with WENO reconstructions of u at x-faces and v at y-faces
- * (FP64 lane; ccs_init returns CCS_ERR_UNSUPPORTED for it on the mixed lane). */
+ * (both lanes). */
 enum { CCS_EDISS_ZERO = 0, CCS_EDISS_RECONSTRUCT = 1 };
 
 /* spatial operator.  The reference ships four interchangeable modules of the same

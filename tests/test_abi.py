@@ -117,14 +117,5 @@ def test_autotune_entry_points_reject_null_handle_without_device():
     assert lib.ccs_get_variant(None, None, None, None) == L.CCS_ERR_ARG
 
 
-def test_mixed_lane_rejects_e_reconstruction_without_device():
-    mesh = M.Mesh(8, 3)
-    mv = mesh.view()
-    h = C.c_void_p()
-    rc = L.lib().ccs_init(C.byref(_cfg(precision=1, e_dissipation=1)), C.byref(mv), C.byref(h))
-    assert rc == L.CCS_ERR_UNSUPPORTED
-    assert not h.value
-
-
 def test_check_state_rejects_null_handle_without_device():
     assert L.lib().ccs_check_state(None, None) == L.CCS_ERR_ARG
