@@ -346,7 +346,7 @@ def main():
     ap.add_argument("--tile-variant", type=int, default=-1,
                     help="mixed-lane tile variant of the C384 run (-1: autotuner)")
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--N", type=int, default=N_BENCH)
