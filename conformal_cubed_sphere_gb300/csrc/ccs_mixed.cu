@@ -283,7 +283,8 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
         const float pB = fmaf(0.5f, pH + hc, phibar);
         const float lm = fabsf(uB) + sqrt_approx(fmaxf(lam_cur * pB, 0.f));
         const float gF = 0.5f * fmaf(-lm, dP1 + DPm - pDPp, dF1 + pDFp + DFm);
-        const float gE = EDISS ? 0.5f * fmaf(-lm, dU1 + DUm - pDUp, dE1 + pDEp + DEm)
+        // (the wind is carried as u / a^2 and E unscaled: the dissipation takes a^2 back)
+        const float gE = EDISS ? 0.5f * fmaf(-lm * st.a2, dU1 + DUm - pDUp, dE1 + pDEp + DEm)
                                : 0.5f * (dE1 + pDEp + DEm);
         if (XDIR) {
           S.gx[0][line][fi] = gF;
