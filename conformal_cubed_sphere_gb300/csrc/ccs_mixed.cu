@@ -252,17 +252,12 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
     const float qn = hn * sn;
     const float dF3 = Fn - Flast, dE3 = En - Elast, dP3 = fmaf(phibar, sn - slast, qn - qlast);
     float DFp, DFm, DEp, DEm, DPp, DPm;
-#ifdef CCS_MIXED_SCALAR_WENO
-    weno_d(dF0, dF1, dF2, dF3, epsF, DFp, DFm);
-    weno_d(dP0, dP1, dP2, dP3, epsP, DPp, DPm);
-#else
     {
       float2 Dp2, Dm2;
       weno_d2(make_float2(dF0, dP0), make_float2(dF1, dP1), make_float2(dF2, dP2), make_float2(dF3, dP3),
               make_float2(epsF, epsP), Dp2, Dm2);
       DFp = Dp2.x; DPp = Dp2.y; DFm = Dm2.x; DPm = Dm2.y;
     }
-#endif
     float DUp = 0.f, DUm = 0.f, Un = 0.f, dU3 = 0.f;
     if constexpr (EDISS) {
       Un = Uw[on];
