@@ -256,13 +256,20 @@ def _batch_time(batch, torch, steps: int):
 
 
 def run_ensemble(args, torch):
-    """64 members at C96 (seed + k, RMS 150-250 m, wind 30-50 m/s), mixed lane, one
-    launch per RK stage for all members, graph-captured; against the same members
-    advanced one after another through their own handles."""
+    """`members` members at C96 per GPU (seed + k, RMS 150-250 m, wind 30-50 m/s),
+    mixed lane, one launch per RK stage for all of a rank's members, graph-captured;
+    against the same members advanced one after another through their own handles.
+    Under torchrun the ensemble is members x ranks, sharded round robin by member
+    with no collective on the data path (weak scaling)."""
     from conformal_cubed_sphere_gb300 import model as M
-    n, N = args.members, 96
+    from conformal_cubed_sphere_gb300.parallel import shard_members, slowest_rank_seconds
+    ws, rank, _ = _dist()
+    N = 96
+    total = args.members * ws
+    mine = shard_members(total, rank, ws)
+    n = len(mine)
     mesh = M.Mesh(N, HALO)
-    states = [M.ensemble_member_state(mesh, k, seed=SEED) for k in range(n)]
+    states = [M.ensemble_member_state(mesh, k, seed=SEED) for k in mine]
     dts = [M.cfl_dt(mesh, st, 0.5) for st in states]
     phibar = 8000.0 * mesh.gravity
     owner = M.Stepper(mesh, dts[0], precision="mixed", phi_mean=phibar)
@@ -273,29 +280,37 @@ def run_ensemble(args, torch):
         m.autotune(reps=5)  # timed once for the grid, then the cached choice
     batch = M.Batch(members)
     batch.step(max(args.warmup, 3))
-    t_batch = _batch_time(batch, torch, args.steps)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    t_batch = slowest_rank_seconds(_batch_time(batch, torch, args.steps))
     # sequential: the same members, one handle after another
     for m in members:
         m.step(1)
     torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for m in members:
         m.step(args.steps)
-    t_seq = time.perf_counter() - t0
-    cells = 6 * N * N * n
-    rate = n * args.steps / t_batch
+    t_seq = slowest_rank_seconds(time.perf_counter() - t0)
+    if rank != 0:
+        return
+    cells = 6 * N * N * total
+    rate = total * args.steps / t_batch
     print(json.dumps({
-        "metric": "ensemble member-steps/s (64 x C96, mixed lane)", "value": rate, "unit": "member-steps/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_batch / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 metric transforms)",
-        "data": "synthetic (seeded spherical harmonics)",
-        "config": {"workload": f"{n} members at C{N}, seed+k, RMS U[150,250] m, wind U[30,50] m/s, RK4, CFL 0.5",
+        "metric": f"ensemble member-steps/s ({args.members} x C96 per GPU, mixed lane)", "value": rate,
+        "unit": "member-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 metric transforms)", "data": "synthetic (seeded spherical harmonics)",
+        "config": {"workload": f"{total} members at C{N} ({args.members} per GPU, sharded by member), seed+k, "
+                               "RMS U[150,250] m, wind U[30,50] m/s, RK4, CFL 0.5",
                    "l2": "inputs larger than L2 (all members' state)"},
         "cell_steps_per_s": cells * args.steps / t_batch,
-        "sequential": {"value": n * args.steps / t_seq, "unit": "member-steps/s",
+        "sequential": {"value": total * args.steps / t_seq, "unit": "member-steps/s",
                        "how": "each member's own handle (graph per step), one after another, host-timed"},
         "batch_over_sequential": t_seq / t_batch,
-        "hbm": {"alg_GBs": ALG_BYTES_MIXED * cells * args.steps / t_batch / 1e9, "peak": _peaks()[0]},
+        "hbm": {"alg_GBs": ALG_BYTES_MIXED * cells * args.steps / t_batch / 1e9, "peak": _peaks()[0] * ws},
     }))
 
 
@@ -359,15 +374,15 @@ def main():
     ws, rank, local = _dist()
     import torch
     torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     if args.workload == "ensemble":
         run_ensemble(args, torch)
         return
     if args.workload == "uneven":
         run_uneven(args, torch)
         return
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from conformal_cubed_sphere_gb300 import model as M
 
     mesh, s, dt = build_case(args.N)
