@@ -144,6 +144,31 @@ static int validate_config(const ccs_config *c) {
   return CCS_OK;
 }
 
+// The mixed lane keeps one copy of sqrtG and G^-1 for all six panels: true of a
+// cube map (the panels are rotations of one face map, halo cells included), checked
+// here to 1e-12 relative (G^-1 entries relative to its diagonal) on every cell
+// outside the corner blocks.
+static bool panels_share_metric(int N, int h, const ccs_mesh_view *m) {
+  const int nh = N + 2 * h;
+  const size_t np = (size_t)nh * nh;
+  auto close = [](double a, double b) { return std::fabs(a - b) <= 1e-12 * std::fmax(std::fabs(a), std::fabs(b)); };
+  for (int j = 1 - h; j <= N + h; j++)
+    for (int i = 1 - h; i <= N + h; i++) {
+      if ((i < 1 || i > N) && (j < 1 || j > N)) continue;
+      const size_t r0 = (size_t)(i + h - 1) + (size_t)nh * (j + h - 1);
+      for (int p = 1; p < 6; p++) {
+        const size_t r = r0 + np * p;
+        if (!close(m->sqrtG[r], m->sqrtG[r0])) return false;
+        // entries against the matrix's scale (off-diagonals vanish on the centre lines)
+        const double *a = &m->matrixIG[4 * r], *b = &m->matrixIG[4 * r0];
+        const double scale = std::fabs(b[0]) + std::fabs(b[3]);
+        for (int q = 0; q < 4; q++)
+          if (!(std::fabs(a[q] - b[q]) <= 1e-12 * scale)) return false;
+      }
+    }
+  return true;
+}
+
 // matmul of two 2x2 column-major matrices as gfortran inlines it (c = 0; c += ...)
 static void matmul22(const double *X, const double *Y, double *M) {
   for (int c = 0; c < 2; c++)
@@ -453,6 +478,9 @@ int ccs_init(const ccs_config *cfg, const ccs_mesh_view *mesh, ccs_handle **out)
   if (!mesh || !mesh->sqrtG || !mesh->matrixG || !mesh->matrixIG || !mesh->matrixA || !mesh->matrixIA ||
       !mesh->f || !mesh->phis)
     return CCS_ERR_ARG;
+  if (out) *out = nullptr;
+  if (validate_config(cfg)) return CCS_ERR_ARG;
+  if (cfg->precision == CCS_MIXED && !panels_share_metric(cfg->N, cfg->halo, mesh)) return CCS_ERR_UNSUPPORTED;
   ccs_handle *h = nullptr;
   int rc = init_common(cfg, out, &h);
   if (rc) return rc;

@@ -119,3 +119,29 @@ def test_autotune_entry_points_reject_null_handle_without_device():
 
 def test_check_state_rejects_null_handle_without_device():
     assert L.lib().ccs_check_state(None, None) == L.CCS_ERR_ARG
+
+
+def test_mixed_lane_needs_a_cube_symmetric_metric_without_device():
+    """The mixed lane keeps one metric for all panels; a mesh whose panels differ is
+    refused before any device call (the FP64 lane takes any mesh)."""
+    mesh = M.Mesh(8, 3)
+    mesh.sqrtG = mesh.sqrtG.copy()
+    mesh.field(mesh.sqrtG)[5, 5, 2] *= 1.0 + 1e-9
+    mv = mesh.view()
+    h = C.c_void_p()
+    rc = L.lib().ccs_init(C.byref(_cfg(precision=1)), C.byref(mv), C.byref(h))
+    assert rc == L.CCS_ERR_UNSUPPORTED and not h.value
+
+
+def test_generated_meshes_pass_the_panel_symmetry_check():
+    """Every generated mesh (conformal, halos 3 and 5) passes the mixed lane's
+    one-metric-for-all-panels check: ccs_init gets past it to the device set-up
+    (no GPU here: CCS_ERR_NODEVICE or a CUDA error, not CCS_ERR_UNSUPPORTED)."""
+    for N, h in ((6, 3), (12, 5), (32, 3)):
+        mesh = M.Mesh(N, h)
+        mv = mesh.view()
+        hd = C.c_void_p()
+        rc = L.lib().ccs_init(C.byref(_cfg(N=N, halo=h, precision=1)), C.byref(mv), C.byref(hd))
+        assert rc != L.CCS_ERR_UNSUPPORTED and rc != L.CCS_ERR_ARG, rc
+        if rc == 0:
+            L.lib().ccs_destroy(hd)
