@@ -9,8 +9,10 @@ FP32/FP64 lane; the FP64 parity lane is measured beside it on the same state.
   value      device-timed throughput, inputs resident in HBM, L2 flushed between
              timed steps (CUDA events on the library's own stream)
   e2e        the same metric through the C ABI with host buffers: every step is
-             ccs_set_state (pinned host -> device) + ccs_step(1) + ccs_get_state
-             (device -> pinned host)
+             ccs_set_state_async of its input (pinned host -> device) +
+             ccs_step_async(1) + ccs_get_state_async of its result (device ->
+             pinned host), one ccs_sync at the end, so one step's copies overlap
+             the neighbouring steps; the synchronous calls are reported beside it
   roofline   the mixed stage kernel's average launch duration against the
              measured HBM copy bandwidth
   cpu_baseline  the CPU FP64 oracle (a restatement of the reference step) on the
@@ -19,7 +21,11 @@ FP32/FP64 lane; the FP64 parity lane is measured beside it on the same state.
 --impl reference times only the reference CPU step (the oracle) on the same
 workload and prints its own line.  Under torchrun (N > 1) every rank advances
 its own C384 replica (the single-member step does not shard): value is the
-total over ranks divided by the slowest rank's time.
+total over ranks divided by the slowest rank's time.  --workload ensemble (64 x
+C96 members per GPU, sharded by member across ranks) and --workload uneven
+(16 x C48 + 8 x C96 + 4 x C192 + 1 x C384, FP64 and mixed members together)
+print their own lines.  Tile shapes come from the autotuner (--tile-variant
+pins the mixed one for profiling runs).
 """
 from __future__ import annotations
 
