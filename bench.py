@@ -163,7 +163,8 @@ def e2e_rate(stepper, mesh, state, steps: int, torch):
     """Per step: ccs_set_state of the step's input (pinned host -> device), ccs_step(1)
     and ccs_get_state of its result (device -> pinned host).  Two loops: the async
     entry points (upload of step k+1 and download of result k overlap the steps; two
-    result buffers in turn), and the synchronous calls one after another."""
+    result buffers in turn), and the synchronous calls one after another.  Returns
+    the two loops' wall times and the bytes moved per step each way."""
     from conformal_cubed_sphere_gb300 import model as M
     pin_in = {k: torch.from_numpy(state[k].copy()).pin_memory() for k in M.STATE_FIELDS}
     sin = M.State({k: v.numpy() for k, v in pin_in.items()})
@@ -196,7 +197,7 @@ def e2e_rate(stepper, mesh, state, steps: int, torch):
         stepper.get_state(outs[0])
     el_sync = time.perf_counter() - t0
     nb = mesh.ncell * 8
-    return cells * steps / el_async, cells * steps / el_sync, n_in * nb, n_out * nb
+    return el_async, el_sync, n_in * nb, n_out * nb
 
 
 def cpu_baseline(mesh, state, dt, seconds=10.0):
@@ -441,7 +442,12 @@ def main():
     mixed2 = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
     mixed2.set_state(s)
     mixed2.set_variant(mixed.variant[0])
-    e2e, e2e_sync, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
+    if ws > 1:
+        torch.distributed.barrier()
+    el_async, el_sync, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
+    # every rank moves its own replica's data over its own host link: whole-job rate
+    e2e = ws * cells * e2e_steps / slowest_rank_seconds(el_async)
+    e2e_sync = ws * cells * e2e_steps / slowest_rank_seconds(el_sync)
 
     if rank != 0:
         return
