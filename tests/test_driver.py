@@ -147,3 +147,20 @@ def test_cpp_driver_matches_the_python_api(tmp_path):
     m = ~mesh.corner_mask()
     for k, name in enumerate(("phiG", "u", "v")):
         assert np.array_equal(got[k][m].view(np.int64), ref[name][m].view(np.int64)), name
+
+
+def test_cpp_driver_reads_a_mesh_file(tmp_path):
+    """--mesh-file: the driver takes N from the raw-binary mesh file (host only, --plan)."""
+    import subprocess
+
+    from conformal_cubed_sphere_gb300 import model as M
+
+    path = tmp_path / "c10.ccsmesh"
+    M.Mesh(10, 3).save(path)
+    r = subprocess.run([_driver_binary(), "--mesh-file", str(path), "--plan", "--run-days", "0", "--run-hours",
+                        "1", "--dt", "600", "--history-interval", "1800"], capture_output=True, text=True,
+                       check=True)
+    assert " N 10 halo 3 dt 600 nsteps 6 outputs 2" in r.stdout
+    bad = subprocess.run([_driver_binary(), "--mesh-file", str(tmp_path / "absent"), "--plan"],
+                         capture_output=True, text=True)
+    assert bad.returncode != 0 and "mesh file" in bad.stderr
