@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace ccs {
@@ -280,6 +281,25 @@ extern "C" int ccs_ghost_map(int N, int halo, int64_t *src_index) {
 // ---------------------------------------------------------------------------
 namespace {
 
+// f(0) .. f(n - 1) on the host's hardware threads (round robin); f must only write
+// to the slots its argument owns.
+template <class F>
+void parallel_for(int n, F &&f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = (int)std::max(1u, std::min(hw ? hw : 1u, 64u));
+  if (nt == 1 || n < 2) {
+    for (int r = 0; r < n; r++) f(r);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nt; t++)
+    pool.emplace_back([&, t]() {
+      for (int r = t; r < n; r += nt) f(r);
+    });
+  for (auto &th : pool) th.join();
+}
+
+
 using cd = std::complex<double>;
 
 // Equiangular gnomonic: angle coordinates (X, Y) * pi/4.
@@ -550,10 +570,39 @@ extern "C" int ccs_mesh_generate(int N, int map, double *lon_deg, double *lat_de
   std::vector<cd> cw((size_t)half * half), cf((size_t)half * half);
   std::vector<char> have((size_t)half * half, 0);
   auto dist_index = [N](int i) { return (std::abs(2 * i - N - 1) - (N % 2 == 0 ? 1 : 0)) / 2; };
-  for (int j = 1; j <= N; j++)
+  auto local_x = [dx_deg](int i) { return ((2 * i - 1) * dx_deg / 2. - 45.) * (2. / 90.); };
+  if (map == CCS_MAP_CONFORMAL) {
+    // the fundamental-triangle argument of each key, taken from the first cell (in
+    // row order) that needs it, then all keys solved on the host's threads
+    std::vector<double> ka((size_t)half * half), kb((size_t)half * half);
+    std::vector<size_t> keys;
+    for (int j = 1; j <= N; j++)
+      for (int i = 1; i <= N; i++) {
+        double a = std::fabs(local_x(i)), b = std::fabs(local_x(j));
+        if (b > a) std::swap(a, b);
+        if (a == 0. && b == 0.) continue;  // the face centre needs no solve
+        int ia = dist_index(i), ib = dist_index(j);
+        if (ia < ib) std::swap(ia, ib);
+        const size_t key = (size_t)ia * half + ib;
+        if (have[key]) continue;
+        have[key] = 1;
+        ka[key] = a;
+        kb[key] = b;
+        keys.push_back(key);
+      }
+    std::vector<char> ok(keys.size(), 0);
+    parallel_for((int)keys.size(), [&](int n) {
+      const size_t key = keys[n];
+      ok[n] = C.fundamental(cd(ka[key], kb[key]), &cw[key], &cf[key]) ? 1 : 0;
+    });
+    for (char o : ok)
+      if (!o) return CCS_ERR_MESH;
+  }
+  std::vector<char> row_ok(N, 1);
+  parallel_for(N, [&](int jr) {
+    const int j = jr + 1;
     for (int i = 1; i <= N; i++) {
-      const double X = ((2 * i - 1) * dx_deg / 2. - 45.) * (2. / 90.);
-      const double Y = ((2 * j - 1) * dx_deg / 2. - 45.) * (2. / 90.);
+      const double X = local_x(i), Y = local_x(j);
       double *q = &lp[9 * ((size_t)(i - 1) + (size_t)N * (j - 1))];
       if (map == CCS_MAP_GNOMONIC_EQUIANGULAR) {
         gnomonic_local(X, Y, q, q + 3, q + 6);
@@ -562,17 +611,16 @@ extern "C" int ccs_mesh_generate(int N, int map, double *lon_deg, double *lat_de
       int ia = dist_index(i), ib = dist_index(j);
       if (ia < ib) std::swap(ia, ib);
       const size_t key = (size_t)ia * half + ib;
-      auto fund = [&](double a, double b, cd *w, cd *fp) {
-        if (!have[key]) {
-          if (!C.fundamental(cd(a, b), &cw[key], &cf[key])) return false;
-          have[key] = 1;
-        }
+      auto fund = [&](double, double, cd *w, cd *fp) {
         *w = cw[key];
         *fp = cf[key];
         return true;
       };
-      if (!conformal_local(C, X, Y, q, q + 3, q + 6, fund)) return CCS_ERR_MESH;
+      if (!conformal_local(C, X, Y, q, q + 3, q + 6, fund)) row_ok[jr] = 0;
     }
+  });
+  for (char o : row_ok)
+    if (!o) return CCS_ERR_MESH;
   for (int p = 1; p <= 6; p++)
     for (int j = 1; j <= N; j++)
       for (int i = 1; i <= N; i++) {
@@ -734,7 +782,8 @@ struct ShField {
   // value and d/dlon at (lon, lat)
   void eval(double lon, double lat, double *val, double *dlon) const {
     const double mu = std::sin(lat), cl = std::cos(lat);
-    std::vector<double> P((size_t)(L + 1) * (L + 1), 0.);
+    thread_local std::vector<double> P;
+    P.assign((size_t)(L + 1) * (L + 1), 0.);
     auto at = [&](int l, int m) -> double & { return P[(size_t)l * (L + 1) + m]; };
     at(0, 0) = 1.;
     for (int m = 1; m <= L; m++) at(m, m) = std::sqrt((2. * m + 1.) / (2. * m)) * cl * at(m - 1, m - 1);
@@ -841,30 +890,34 @@ extern "C" int ccs_initial_condition(int N, int halo, double radius, double grav
   if (oro) foro.draw(prm->lmax_oro, rng);
   std::vector<double> hp(nc, 0.), us(nc, 0.), vs(nc, 0.), hs(nc, 0.);
   std::vector<char> live(nc, 0);
-  for (int p = 1; p <= 6; p++)
-    for (int j = 1 - halo; j <= N + halo; j++)
-      for (int i = 1 - halo; i <= N + halo; i++) {
-        const bool ci = i < 1 || i > N, cj = j < 1 || j > N;
-        if (ci && cj) continue;  // corner block
-        const size_t k = H.at(i, j, p);
-        live[k] = 1;
-        double v, d;
-        fh.eval(lon[k], lat[k], &v, &d);
-        hp[k] = v;
-        // u = -(1/a) dpsi/dlat (central difference, step 1e-5 rad); v = dpsi/dlon / (a cos lat)
-        const double dl = 1e-5;
-        double pp, pm, dd;
-        fpsi.eval(lon[k], lat[k] + dl, &pp, &dd);
-        fpsi.eval(lon[k], lat[k] - dl, &pm, &dd);
-        double pc, dlon;
-        fpsi.eval(lon[k], lat[k], &pc, &dlon);
-        us[k] = -(pp - pm) / (2. * dl);
-        vs[k] = dlon / std::cos(lat[k]);
-        if (oro) {
-          foro.eval(lon[k], lat[k], &v, &d);
-          hs[k] = v;
-        }
+  // every cell's values depend on its own lon/lat only: the rows are shared out
+  // among host threads (the reductions below stay sequential and in order)
+  const int nrows = 6 * (N + 2 * halo);
+  parallel_for(nrows, [&](int row) {
+    const int p = 1 + row / (N + 2 * halo), j = 1 - halo + row % (N + 2 * halo);
+    for (int i = 1 - halo; i <= N + halo; i++) {
+      const bool ci = i < 1 || i > N, cj = j < 1 || j > N;
+      if (ci && cj) continue;  // corner block
+      const size_t k = H.at(i, j, p);
+      live[k] = 1;
+      double v, d;
+      fh.eval(lon[k], lat[k], &v, &d);
+      hp[k] = v;
+      // u = -(1/a) dpsi/dlat (central difference, step 1e-5 rad); v = dpsi/dlon / (a cos lat)
+      const double dl = 1e-5;
+      double pp, pm, dd;
+      fpsi.eval(lon[k], lat[k] + dl, &pp, &dd);
+      fpsi.eval(lon[k], lat[k] - dl, &pm, &dd);
+      double pc, dlon;
+      fpsi.eval(lon[k], lat[k], &pc, &dlon);
+      us[k] = -(pp - pm) / (2. * dl);
+      vs[k] = dlon / std::cos(lat[k]);
+      if (oro) {
+        foro.eval(lon[k], lat[k], &v, &d);
+        hs[k] = v;
       }
+    }
+  });
   double s2 = 0., vmax = 0., o2 = 0.;
   size_t cnt = 0;
   for (int p = 1; p <= 6; p++)
