@@ -271,3 +271,25 @@ def test_health_check_counts_bad_cells(precision):
     F(bad["phi"])[0, 5, 0] = np.nan  # a halo cell: not counted
     g.set_state(bad)
     assert g.check_state() == 2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_corner_blocks_are_never_read(precision):
+    """NaN in every corner-block cell of the input changes nothing outside the corner
+    blocks (both lanes): the step never reads a cell the reference never fills."""
+    mesh, s, dt = seeded_case(16, 3, seed=17, oro=True)
+    poisoned = s.copy()
+    cm = mesh.corner_mask()
+    for k in ("phiG", "u", "v", "phi", "uC", "vC", "zonal_wind", "meridional_wind"):
+        poisoned[k][cm] = np.nan
+    kw = dict(phi_mean=8000.0 * mesh.gravity) if precision == "mixed" else {}
+    out = []
+    for st in (s, poisoned):
+        g = M.Stepper(mesh, dt, precision=precision, **kw)
+        g.set_state(st)
+        g.step(4)
+        assert g.check_state() == 0
+        out.append(g.get_state())
+    m = valid_mask(mesh)
+    for k in CHECK_FIELDS:
+        assert bitwise_equal(out[0][k], out[1][k], m), k
