@@ -105,6 +105,8 @@ SIGNATURES = {
     "ccs_mesh_save": (C.c_int, [C.c_char_p, C.c_int, C.c_int] + [_dp] * 6),
     "ccs_mesh_file_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "ccs_mesh_load": (C.c_int, [C.c_char_p, C.c_int] + [_dp] * 6),
+    "ccs_state_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(StateView)]),
+    "ccs_state_read": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(StateView)]),
     "ccs_last_error": (C.c_char_p, [_vp]),
     "ccs_abi_version": (C.c_int, []),
     "ccs_mesh_generate": (C.c_int, [C.c_int, C.c_int] + [_dp] * 6),

@@ -1,6 +1,7 @@
 // ccs_api.cu -- the C ABI (include/ccs_gpu.h): handles, device buffers, stage
 // descriptors, CUDA-graph capture of a step, state transfer and diagnostics.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -21,6 +22,13 @@ using namespace ccs;
 namespace {
 
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// NVTX range over a host call (named in Nsight Systems / ncu timelines; a no-op when
+// no tool is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 // Health check: counts interior cells whose depth is not positive (NaN included) or
 // whose covariant wind is not finite.  phi = phi0 + hp[c] (FP64 lane: phi0 = 0 and
@@ -534,6 +542,7 @@ void ccs_destroy(ccs_handle *h) {
 }
 
 static int set_state_impl(ccs_handle *h, const ccs_state_view *s, bool sync) {
+  NvtxRange nvtx("ccs_set_state");
   if (!h || !s || !s->phiG || !s->u || !s->v || !s->phi || !s->uC || !s->vC) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
   if (h->cfg.precision == CCS_MIXED) return mixed_set_state(h, s, sync);
@@ -558,6 +567,7 @@ int ccs_set_state(ccs_handle *h, const ccs_state_view *s) { return set_state_imp
 int ccs_set_state_async(ccs_handle *h, const ccs_state_view *s) { return set_state_impl(h, s, false); }
 
 static int get_state_impl(ccs_handle *h, ccs_state_view *s, bool sync) {
+  NvtxRange nvtx("ccs_get_state");
   if (!h || !s) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
   if (h->cfg.precision == CCS_MIXED) return mixed_get_state(h, s, sync);
@@ -586,6 +596,7 @@ int ccs_get_state(ccs_handle *h, ccs_state_view *s) { return get_state_impl(h, s
 int ccs_get_state_async(ccs_handle *h, ccs_state_view *s) { return get_state_impl(h, s, false); }
 
 int ccs_step(ccs_handle *h, int nsteps) {
+  NvtxRange nvtx("ccs_step");
   if (!h || nsteps < 0) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
   if (h->cfg.precision == CCS_MIXED) return mixed_step(h, nsteps, true);
@@ -593,6 +604,7 @@ int ccs_step(ccs_handle *h, int nsteps) {
 }
 
 int ccs_step_async(ccs_handle *h, int nsteps) {
+  NvtxRange nvtx("ccs_step_async");
   if (!h || nsteps < 0) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
   if (h->cfg.precision == CCS_MIXED) return mixed_step(h, nsteps, false);
@@ -643,6 +655,7 @@ int ccs_spatial_operator(ccs_handle *h, double *tp, double *tu, double *tv) {
 }
 
 int ccs_diag(ccs_handle *h, double *mass, double *energy) {
+  NvtxRange nvtx("ccs_diag");
   if (!h) return CCS_ERR_ARG;
   cudaSetDevice(h->cfg.device);
   if (h->cfg.precision == CCS_MIXED) return mixed_diag(h, mass, energy);
@@ -1198,6 +1211,7 @@ extern "C" int ccs_get_variant(ccs_handle *h, int *var, int *tile_x, int *tile_y
 }
 
 extern "C" int ccs_autotune(ccs_handle *h, int reps, int force, int *chosen, double *times_us) {
+  NvtxRange nvtx("ccs_autotune");
   if (!h || reps < 1) return CCS_ERR_ARG;
   if (h->cfg.precision == CCS_MIXED && !h->mixed->have_phibar) return CCS_ERR_ARG;  // state not set
   cudaSetDevice(h->cfg.device);
@@ -1376,6 +1390,7 @@ static int batch_capture(ccs_batch *b, bool with_sw, cudaGraphExec_t *out) {
 }
 
 static int batch_step(ccs_batch *b, int nsteps, bool sync) {
+  NvtxRange nvtx("ccs_batch_step");
   if (!b || nsteps < 0) return CCS_ERR_ARG;
   if (nsteps == 0) return CCS_OK;
   cudaSetDevice(b->device);

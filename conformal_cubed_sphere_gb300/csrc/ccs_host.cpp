@@ -1085,3 +1085,51 @@ extern "C" int ccs_mesh_load(const char *path, int N, double *lon_deg, double *l
   std::fclose(fp);
   return rc;
 }
+
+// ---- checkpoint files -------------------------------------------------------------
+// The reference writes NetCDF history only and has no restart reader.  A checkpoint
+// here is the eight stat fields in the reference's layout behind a small header:
+//   bytes 0-7   magic "CCSSTAT" + '\1'
+//         8-23  int32 version (1), N, halo, number of fields (8)
+//        24-    float64 phiG, u, v, phi, uC, vC, zonal, meridional ((N+2h)^2 * 6 each)
+namespace {
+const char kStateMagic[8] = {'C', 'C', 'S', 'S', 'T', 'A', 'T', '\1'};
+}  // namespace
+
+extern "C" int ccs_state_write(const char *path, int N, int halo, const ccs_state_view *s) {
+  if (!path || N < 1 || halo < 1 || !s || !s->phiG || !s->u || !s->v || !s->phi || !s->uC || !s->vC ||
+      !s->zonal_wind || !s->meridional_wind)
+    return CCS_ERR_ARG;
+  FILE *fp = std::fopen(path, "wb");
+  if (!fp) return CCS_ERR_IO;
+  const size_t n = (size_t)(N + 2 * halo) * (N + 2 * halo) * 6;
+  const int32_t iv[4] = {1, N, halo, 8};
+  bool ok = std::fwrite(kStateMagic, 1, 8, fp) == 8 && std::fwrite(iv, sizeof(int32_t), 4, fp) == 4;
+  const double *f[8] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC, s->zonal_wind, s->meridional_wind};
+  for (int k = 0; k < 8 && ok; k++) ok = std::fwrite(f[k], sizeof(double), n, fp) == n;
+  if (std::fclose(fp) != 0) ok = false;
+  return ok ? CCS_OK : CCS_ERR_IO;
+}
+
+extern "C" int ccs_state_read(const char *path, int N, int halo, ccs_state_view *s) {
+  if (!path || N < 1 || halo < 1 || !s || !s->phiG || !s->u || !s->v || !s->phi || !s->uC || !s->vC ||
+      !s->zonal_wind || !s->meridional_wind)
+    return CCS_ERR_ARG;
+  FILE *fp = std::fopen(path, "rb");
+  if (!fp) return CCS_ERR_IO;
+  char magic[8];
+  int32_t iv[4];
+  int rc = CCS_OK;
+  if (std::fread(magic, 1, 8, fp) != 8 || std::memcmp(magic, kStateMagic, 8) != 0 ||
+      std::fread(iv, sizeof(int32_t), 4, fp) != 4 || iv[0] != 1 || iv[3] != 8)
+    rc = CCS_ERR_IO;
+  else if (iv[1] != N || iv[2] != halo)
+    rc = CCS_ERR_ARG;
+  const size_t n = (size_t)(N + 2 * halo) * (N + 2 * halo) * 6;
+  double *f[8] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC, s->zonal_wind, s->meridional_wind};
+  for (int k = 0; k < 8 && !rc; k++)
+    if (std::fread(f[k], sizeof(double), n, fp) != n) rc = CCS_ERR_IO;
+  if (!rc && std::fgetc(fp) != EOF) rc = CCS_ERR_IO;
+  std::fclose(fp);
+  return rc;
+}

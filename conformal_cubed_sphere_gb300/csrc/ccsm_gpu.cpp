@@ -17,7 +17,8 @@
 // ccsm.F90:60 computes it from stat(old), unless --energy-of-new-state.  --out
 // writes phiG, u, v of the final state (FP64, the reference's array layout, one
 // field after the other).  --plan prints the time settings and output steps and
-// exits without touching a GPU.
+// exits without touching a GPU.  Every output time runs the health check
+// (ccs_check_state) and stops on a state with non-positive depth or non-finite wind.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -210,6 +211,12 @@ int main(int argc, char **argv) {
       if ((rc = ccs_diag(hd, &mass, &tmp))) return done(fail("ccs_diag", rc));
     }
     stepped = it;
+    int64_t nbad = 0;
+    if (ccs_check_state(hd, &nbad) == CCS_ERR_NAN) {
+      std::fprintf(stderr, "ccsm_gpu: step %d: %lld cells with non-positive depth or non-finite wind\n", it,
+                   (long long)nbad);
+      return done(1);
+    }
     // history_write_stat(stat(new)) would write here: ccs_get_state gives stat(new)
     std::printf(" output index/total, MCR, ECR : %zu / %d   %.17g %.17g\n", k + 1, total_output_num,
                 (mass - mass0) / mass0, (energy - energy0) / energy0);

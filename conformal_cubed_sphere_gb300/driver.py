@@ -70,10 +70,13 @@ class OutputRecord:
 
 
 def run(stepper, ts: TimeSettings, on_output: Callable | None = None, energy_of_new_state: bool = False,
-        log: Callable[[str], None] | None = print) -> list[OutputRecord]:
+        log: Callable[[str], None] | None = print, check: bool = True) -> list[OutputRecord]:
     """Advances `stepper` (a model.Stepper whose state is set) through the run of
     `ts`; calls on_output(output_idx, state) at every history time with the state
-    as ccs_get_state returns it (sphere winds included); returns the MCR/ECR records."""
+    as ccs_get_state returns it (sphere winds included); returns the MCR/ECR records.
+    With `check`, every output time also runs the health check (ccs_check_state) and
+    a state with non-positive depth or non-finite wind stops the run with
+    FloatingPointError (the reference has no such check and carries on with NaNs)."""
     if ts.integral_scheme not in ("RK4", "RK3_TVD"):
         raise ValueError(f"integral_scheme {ts.integral_scheme!r}")
     mass0, energy0 = stepper.diag()
@@ -96,6 +99,10 @@ def run(stepper, ts: TimeSettings, on_output: Callable | None = None, energy_of_
             mass = stepper.diag()[0]
         done = it
         idx = k + 2
+        if check:
+            nbad = stepper.check_state()
+            if nbad:
+                raise FloatingPointError(f"step {it}: {nbad} cells with non-positive depth or non-finite wind")
         if on_output is not None:
             on_output(idx, stepper.get_state())
         rec = OutputRecord(idx, it, (mass - mass0) / mass0, (energy - energy0) / energy0)

@@ -141,6 +141,19 @@ class State:
     def __setitem__(self, k, v):
         self.arrays[k] = v
 
+    def save(self, path, mesh: "Mesh") -> None:
+        """Checkpoint file of this state (ccs_state_write)."""
+        sv = self.view()
+        L.check(L.lib().ccs_state_write(str(path).encode(), mesh.N, mesh.halo, C.byref(sv)), "ccs_state_write")
+
+    @classmethod
+    def load(cls, path, mesh: "Mesh") -> "State":
+        """A state from a checkpoint file of this mesh's size (ccs_state_read)."""
+        st = cls.zeros(mesh)
+        sv = st.view()
+        L.check(L.lib().ccs_state_read(str(path).encode(), mesh.N, mesh.halo, C.byref(sv)), "ccs_state_read")
+        return st
+
     def copy(self) -> "State":
         return State({k: v.copy() for k, v in self.arrays.items()})
 

@@ -281,6 +281,15 @@ int ccs_mesh_file_info(const char *path, int *N, int *map);
 int ccs_mesh_load(const char *path, int N, double *lon_deg, double *lat_deg, double *x, double *y,
                   double *z, double *jab);
 
+/* Checkpoint files (the reference writes NetCDF history only and has no restart):
+ * the eight stat fields phiG, u, v, phi, uC, vC, zonal_wind, meridional_wind in the
+ * reference's layout behind a header (magic "CCSSTAT\1", int32 version 1, N, halo,
+ * 8).  ccs_state_read fails with CCS_ERR_ARG when the file's N or halo differ and
+ * CCS_ERR_IO on a missing, short, over-long or foreign file.  Writing the state of an
+ * FP64-lane handle and setting it again resumes the run bit for bit. */
+int ccs_state_write(const char *path, int N, int halo, const ccs_state_view *s);
+int ccs_state_read(const char *path, int N, int halo, ccs_state_view *s);
+
 /* io_mod.F90:119-220, 295-306: halo fill of the samples and per-cell G = J^T J,
  * G^-1, sqrt(det G), A = S J, A^-1 (pole cases included), f = 2 Omega sin(lat).
  * Outputs are (ics:ice, ics:ice, 6) / (2, 2, ...) arrays; corner-block matrices are

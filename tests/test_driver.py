@@ -46,6 +46,9 @@ class _FakeStepper:
     def get_state(self):
         return self.n
 
+    def check_state(self):
+        return 0 if self.n < 1000 else 7
+
 
 def test_run_chunks_steps_and_uses_old_state_energy():
     ts = D.TimeSettings(dt=600.0, run_days=0, run_hours=2, history_interval=1800)
@@ -164,3 +167,14 @@ def test_cpp_driver_reads_a_mesh_file(tmp_path):
     bad = subprocess.run([_driver_binary(), "--mesh-file", str(tmp_path / "absent"), "--plan"],
                          capture_output=True, text=True)
     assert bad.returncode != 0 and "mesh file" in bad.stderr
+
+
+def test_run_stops_on_a_bad_state():
+    class Blowup(_FakeStepper):
+        def check_state(self):
+            return 3 if self.n >= 6 else 0
+
+    ts = D.TimeSettings(dt=600.0, run_days=0, run_hours=2, history_interval=1800)
+    with pytest.raises(FloatingPointError, match="step 6: 3 cells"):
+        D.run(Blowup(), ts, log=None)
+    assert len(D.run(Blowup(), ts, log=None, check=False)) == 4
