@@ -33,6 +33,7 @@ CCS_MAX_VARIANTS = 4
 CCS_OP_WENO, CCS_OP_CENTRAL2, CCS_OP_CENTRAL4, CCS_OP_CENTRAL6 = 0, 2, 4, 6
 CCS_MAP_GNOMONIC_EQUIANGULAR = 0
 CCS_MAP_CONFORMAL = 1
+CCS_MESH_POLE_INVERSE = 1
 CCS_IC_CASE2 = 2
 CCS_IC_CASE5 = 5
 CCS_IC_CASE6 = 6
@@ -111,6 +112,7 @@ SIGNATURES = {
     "ccs_abi_version": (C.c_int, []),
     "ccs_mesh_generate": (C.c_int, [C.c_int, C.c_int] + [_dp] * 6),
     "ccs_mesh_derive": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double] + [_dp] * 16),
+    "ccs_mesh_derive_ex": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int] + [_dp] * 16),
     "ccs_initial_condition": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                         C.POINTER(ICParams)] + [_dp] * 8),
     "ccs_state_from_sphere": (C.c_int, [C.c_int, C.c_int, C.POINTER(MeshView), C.POINTER(StateView)]),

@@ -645,11 +645,34 @@ extern "C" int ccs_mesh_generate(int N, int map, double *lon_deg, double *lat_de
 }
 
 // io_mod.F90:119-220 and 295-306.
+static int mesh_derive(int N, int halo, double radius, double omega, int flags, const double *lon_deg,
+                       const double *lat_deg, const double *xc, const double *yc, const double *zc,
+                       const double *jab_c, double *sqrtG, double *G, double *IG, double *A, double *IA, double *f,
+                       double *lon_out, double *lat_out, double *sinlat_out, double *coslat_out);
+
 extern "C" int ccs_mesh_derive(int N, int halo, double radius, double omega, const double *lon_deg,
                                const double *lat_deg, const double *xc, const double *yc, const double *zc,
                                const double *jab_c, double *sqrtG, double *G, double *IG, double *A, double *IA,
                                double *f, double *lon_out, double *lat_out, double *sinlat_out,
                                double *coslat_out) {
+  return mesh_derive(N, halo, radius, omega, 0, lon_deg, lat_deg, xc, yc, zc, jab_c, sqrtG, G, IG, A, IA, f,
+                     lon_out, lat_out, sinlat_out, coslat_out);
+}
+
+extern "C" int ccs_mesh_derive_ex(int N, int halo, double radius, double omega, int flags,
+                                  const double *lon_deg, const double *lat_deg, const double *xc,
+                                  const double *yc, const double *zc, const double *jab_c, double *sqrtG,
+                                  double *G, double *IG, double *A, double *IA, double *f, double *lon_out,
+                                  double *lat_out, double *sinlat_out, double *coslat_out) {
+  if (flags & ~CCS_MESH_POLE_INVERSE) return CCS_ERR_ARG;
+  return mesh_derive(N, halo, radius, omega, flags, lon_deg, lat_deg, xc, yc, zc, jab_c, sqrtG, G, IG, A, IA, f,
+                     lon_out, lat_out, sinlat_out, coslat_out);
+}
+
+static int mesh_derive(int N, int halo, double radius, double omega, int flags, const double *lon_deg,
+                       const double *lat_deg, const double *xc, const double *yc, const double *zc,
+                       const double *jab_c, double *sqrtG, double *G, double *IG, double *A, double *IA, double *f,
+                       double *lon_out, double *lat_out, double *sinlat_out, double *coslat_out) {
   if (N < 1 || halo < 1 || !lon_deg || !lat_deg || !xc || !yc || !zc || !jab_c || !sqrtG || !G || !IG || !A ||
       !IA || !f)
     return CCS_ERR_ARG;
@@ -715,7 +738,7 @@ extern "C" int ccs_mesh_derive(int N, int halo, double radius, double omega, con
             for (int k = 0; k < 3; k++) s = s + S[r + 2 * k] * J[k + 3 * c];
             a[r + 2 * c] = s;
           }
-        if (std::fabs(la * kR2D) != 90) {
+        if (std::fabs(la * kR2D) != 90 || (flags & CCS_MESH_POLE_INVERSE)) {
           if (!brinv2(a, ia)) return CCS_ERR_MESH;
         } else {
           double IA1[4];

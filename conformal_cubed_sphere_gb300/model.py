@@ -41,7 +41,7 @@ class Mesh:
 
     def __init__(self, N: int, halo: int = 3, radius: float = RADIUS, omega: float = OMEGA,
                  gravity: float = GRAVITY, phis: np.ndarray | None = None, cube_map: str = "conformal",
-                 mesh_file: str | None = None):
+                 mesh_file: str | None = None, pole_inverse: bool = False):
         lib = L.lib()
         if mesh_file is not None:
             fn, fmap = C.c_int(), C.c_int()
@@ -78,11 +78,14 @@ class Mesh:
         self.lat = np.zeros(nc)
         self.sinlat = np.zeros(nc)
         self.coslat = np.zeros(nc)
-        L.check(lib.ccs_mesh_derive(self.N, self.halo, self.radius, self.omega, _ptr(f["lon"]), _ptr(f["lat"]),
-                                    _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"]), _ptr(self.sqrtG),
-                                    _ptr(self.matrixG), _ptr(self.matrixIG), _ptr(self.matrixA),
-                                    _ptr(self.matrixIA), _ptr(self.f), _ptr(self.lon), _ptr(self.lat),
-                                    _ptr(self.sinlat), _ptr(self.coslat)), "ccs_mesh_derive")
+        # pole_inverse: A^-1 of a cell centred on a pole (odd N) by inversion instead of
+        # the reference's analytic formula (ccs_mesh_derive_ex, CCS_MESH_POLE_INVERSE)
+        flags = L.CCS_MESH_POLE_INVERSE if pole_inverse else 0
+        L.check(lib.ccs_mesh_derive_ex(self.N, self.halo, self.radius, self.omega, flags, _ptr(f["lon"]),
+                                       _ptr(f["lat"]), _ptr(f["x"]), _ptr(f["y"]), _ptr(f["z"]), _ptr(f["jab"]),
+                                       _ptr(self.sqrtG), _ptr(self.matrixG), _ptr(self.matrixIG),
+                                       _ptr(self.matrixA), _ptr(self.matrixIA), _ptr(self.f), _ptr(self.lon),
+                                       _ptr(self.lat), _ptr(self.sinlat), _ptr(self.coslat)), "ccs_mesh_derive")
         # dx = dy = (90/N) degrees in radians, as io_mod.F90:54-55 converts them
         self.dx = (90.0 / self.N) * D2R
         self.dy = self.dx

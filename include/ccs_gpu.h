@@ -300,6 +300,19 @@ int ccs_mesh_derive(int N, int halo, double radius, double omega,
                     double *matrixG, double *matrixIG, double *matrixA, double *matrixIA,
                     double *f, double *lon, double *lat, double *sinlat, double *coslat);
 
+/* ccs_mesh_derive with options.  CCS_MESH_POLE_INVERSE: at a cell centred on a pole
+ * (odd N) A^-1 is the inverse of A, like at every other cell, instead of the
+ * reference's analytic formula (io_mod.F90:190-210), which multiplies the
+ * longitude rotation by the radius where every other A^-1 scales as 1/radius and
+ * makes an odd-N run blow up in its first step.  Not the reference's arithmetic:
+ * off by default (ccs_mesh_derive). */
+enum { CCS_MESH_POLE_INVERSE = 1 };
+int ccs_mesh_derive_ex(int N, int halo, double radius, double omega, int flags,
+                       const double *lon_deg, const double *lat_deg, const double *x,
+                       const double *y, const double *z, const double *jab, double *sqrtG,
+                       double *matrixG, double *matrixIG, double *matrixA, double *matrixIA,
+                       double *f, double *lon, double *lat, double *sinlat, double *coslat);
+
 /* Initial states: the reference test cases of test_case_mod.F90 (2: steady zonal
  * geostrophic flow :61-95, 5: isolated mountain :98-144, 6: Rossby-Haurwitz wave
  * :147-204) and a seeded random state of spherical harmonics. */

@@ -293,3 +293,23 @@ def test_pole_cell_inverse_follows_the_reference_formula():
         assert np.allclose(IA[:, :, c, c, p], want, rtol=1e-15, atol=0)
     # an off-pole cell: A^-1 is the inverse of A, of order 1/radius
     assert np.max(np.abs(IA[:, :, c + 1, c, 4])) < 1e-5
+
+
+def test_pole_inverse_option_inverts_a_at_the_poles():
+    """CCS_MESH_POLE_INVERSE: the pole cells' A^-1 is the inverse of A (scale 1/radius),
+    every other cell unchanged, and odd-N states come out with covariant winds of
+    the usual size."""
+    N, h = 5, 3
+    ref, fix = M.Mesh(N, h), M.Mesh(N, h, pole_inverse=True)
+    A = fix.matrixA.reshape((2, 2, -1), order="F")
+    IA = fix.matrixIA.reshape((2, 2, -1), order="F")
+    pole = np.abs(np.abs(fix.lat) - np.pi / 2) < 1e-12
+    pole &= ~fix.corner_mask()
+    assert pole.sum() >= 2  # the two pole cells and the halo copies of them
+    for c in np.nonzero(pole)[0]:
+        assert np.allclose(A[:, :, c] @ IA[:, :, c], np.eye(2), atol=1e-12)
+    same = ~pole
+    keep = np.repeat(same, 4)
+    assert np.array_equal(ref.matrixIA[keep], fix.matrixIA[keep])
+    s = M.initial_state(fix, kind=L.CCS_IC_SEEDED, seed=4, lmax_oro=8)
+    assert np.max(np.abs(s["u"][~fix.corner_mask()])) < 1e12
