@@ -59,18 +59,6 @@ __device__ __forceinline__ long long abs_bits(double x) {
   return __double_as_longlong(x) & 0x7fffffffffffffffLL;
 }
 
-// x * 2^K, exactly the IEEE product: for a normal x whose product is normal the
-// exponent field moves by K on the integer pipes; zero, subnormal, infinite, NaN and
-// under- or overflowing cases take the FP64 multiply.
-template <int K>
-__device__ __forceinline__ double pow2_mul(double x) {
-  const int hi = __double2hiint(x), lo = __double2loint(x);
-  const int e = (hi >> 20) & 0x7ff;
-  constexpr int lo_e = K < 0 ? 1 - K : 1, hi_e = K > 0 ? 2046 - K : 2046;
-  if ((unsigned)(e - lo_e) <= (unsigned)(hi_e - lo_e)) return __hiloint2double(hi + K * (1 << 20), lo);
-  return x * (K >= 0 ? (double)(1 << K) : 1.0 / (double)(1 << -K));
-}
-
 // WENO_limiter, spatial_operators_mod.F90:282-361.
 template <int DIR>
 __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double q3, double q4) {
@@ -82,26 +70,26 @@ __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double
     s0 = ccs_div_const(Qim2, 3., y3) - 7. / 6. * Qim1 + 11. / 6. * Qi;
     s1 = ccs_div_const(-Qim1, 6., y6) + 5. / 6. * Qi + 1. / 3. * Qip1;
     s2 = ccs_div_const(Qi, 3., y3) + 5. / 6. * Qip1 - 1. / 6. * Qip2;
-    a0 = Qim2 - pow2_mul<1>(Qim1) + Qi;
-    a1 = Qim1 - pow2_mul<1>(Qi) + Qip1;
-    a2 = Qi - pow2_mul<1>(Qip1) + Qip2;
-    b0 = Qim2 - pow2_mul<2>(Qim1) + 3. * Qi;
+    a0 = Qim2 - 2. * Qim1 + Qi;
+    a1 = Qim1 - 2. * Qi + Qip1;
+    a2 = Qi - 2. * Qip1 + Qip2;
+    b0 = Qim2 - 4. * Qim1 + 3. * Qi;
     b1 = Qim1 - Qip1;
-    b2 = 3. * Qi - pow2_mul<2>(Qip1) + Qip2;
+    b2 = 3. * Qi - 4. * Qip1 + Qip2;
   } else {
     s0 = ccs_div_const(Qip2, 3., y3) - 7. / 6. * Qip1 + 11. / 6. * Qi;
     s1 = ccs_div_const(-Qip1, 6., y6) + 5. / 6. * Qi + 1. / 3. * Qim1;
     s2 = ccs_div_const(Qi, 3., y3) + 5. / 6. * Qim1 - 1. / 6. * Qim2;
-    a0 = Qip2 - pow2_mul<1>(Qip1) + Qi;
-    a1 = Qip1 - pow2_mul<1>(Qi) + Qim1;
-    a2 = Qi - pow2_mul<1>(Qim1) + Qim2;
-    b0 = Qip2 - pow2_mul<2>(Qip1) + 3. * Qi;
+    a0 = Qip2 - 2. * Qip1 + Qi;
+    a1 = Qip1 - 2. * Qi + Qim1;
+    a2 = Qi - 2. * Qim1 + Qim2;
+    b0 = Qip2 - 4. * Qip1 + 3. * Qi;
     b1 = Qip1 - Qim1;
-    b2 = 3. * Qi - pow2_mul<2>(Qim1) + Qim2;
+    b2 = 3. * Qi - 4. * Qim1 + Qim2;
   }
-  const double be0 = ccs_div_const(a0 * a0 * 13., 12., y12) + pow2_mul<-2>(b0 * b0);
-  const double be1 = ccs_div_const(a1 * a1 * 13., 12., y12) + pow2_mul<-2>(b1 * b1);
-  const double be2 = ccs_div_const(a2 * a2 * 13., 12., y12) + pow2_mul<-2>(b2 * b2);
+  const double be0 = ccs_div_const(a0 * a0 * 13., 12., y12) + b0 * b0 * 0.25;
+  const double be1 = ccs_div_const(a1 * a1 * 13., 12., y12) + b1 * b1 * 0.25;
+  const double be2 = ccs_div_const(a2 * a2 * 13., 12., y12) + b2 * b2 * 0.25;
   // the betas are sums of squares (never -0 or negative), the taus absolute values
   const long long t40 = abs_bits(be0 - be1), t41 = abs_bits(be1 - be2);
   const double tau5 = fabs(be2 - be0);
@@ -179,7 +167,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
         g22 = st.m.ig22[c];
         phit = phi + st.m.phis[c];
         phitG = phit * st.m.sqrtG[c];
-        const double K = pow2_mul<-1>(u * uC + v * vC);
+        const double K = 0.5 * (u * uC + v * vC);
         E = phit + K;
         Fx = phiG * uC;
         Fy = phiG * vC;
@@ -251,14 +239,13 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
         ga = S.ig22[r + RX]; gb = S.ig22[r];
         pa = S.phit[r + RX]; pb = S.phit[r];
       }
-      const double uBdy = pow2_mul<-1>(a + b);
-      const double phitBdy = pow2_mul<-1>(pa + pb);
-      const double cw = sqrt(pow2_mul<-1>(ga + gb) * phitBdy);
-      const double e1 = uBdy - cw;
-      const double e2 = uBdy + cw;
+      const double uBdy = 0.5 * (a + b);
+      const double phitBdy = 0.5 * (pa + pb);
+      const double e1 = uBdy - sqrt(0.5 * (ga + gb) * phitBdy);
+      const double e2 = uBdy + sqrt(0.5 * (ga + gb) * phitBdy);
       const double mx = abs_bits(e2) > abs_bits(e1) ? fabs(e2) : fabs(e1);
-      rec[0 * NF + face] = pow2_mul<-1>(Fp + Fn - mx * (Pn - Pp));
-      rec[1 * NF + face] = pow2_mul<-1>(Ep + En - mx * (dn - dp));
+      rec[0 * NF + face] = 0.5 * (Fp + Fn - mx * (Pn - Pp));
+      rec[1 * NF + face] = 0.5 * (Ep + En - mx * (dn - dp));
     }
     __syncthreads();
     }  // op == CCS_OP_WENO
@@ -312,9 +299,9 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
               np = y0p + st.c1 * tp; nu = y0u + st.c1 * tu; nv = y0v + st.c1 * tv;
               break;
             case K_RK4_2: {
-              const double ap = st.accphiG[c] + pow2_mul<1>(tp);
-              const double au = st.accu[c] + pow2_mul<1>(tu);
-              const double av = st.accv[c] + pow2_mul<1>(tv);
+              const double ap = st.accphiG[c] + 2. * tp;
+              const double au = st.accu[c] + 2. * tu;
+              const double av = st.accv[c] + 2. * tv;
               st.accphiG[c] = ap; st.accu[c] = au; st.accv[c] = av;
               np = y0p + st.c1 * tp; nu = y0u + st.c1 * tu; nv = y0v + st.c1 * tv;
               break;
