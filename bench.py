@@ -159,37 +159,57 @@ def kernel_launch_avg_ms(stepper, steps: int):
     return ms / max(n, 1), n
 
 
+def pinned_state(M, mesh, torch, order, fill=None):
+    """A model.State whose fields are consecutive slices of one page-locked block, in
+    `order` first (then the remaining fields), optionally filled from `fill`."""
+    names = list(order) + [k for k in M.STATE_FIELDS if k not in order]
+    block = torch.empty(len(names) * mesh.ncell, dtype=torch.float64).pin_memory().numpy()
+    arrays = {}
+    for q, k in enumerate(names):
+        arrays[k] = block[q * mesh.ncell:(q + 1) * mesh.ncell]
+        if fill is not None:
+            arrays[k][:] = fill[k]
+    return M.State(arrays)
+
+
 def e2e_rate(stepper, mesh, state, steps: int, torch):
     """Per step: ccs_set_state of the step's input (pinned host -> device), ccs_step(1)
-    and ccs_get_state of its result (device -> pinned host).  Two loops: the async
-    entry points (upload of step k+1 and download of result k overlap the steps; two
-    result buffers in turn), and the synchronous calls one after another.  Returns
-    the two loops' wall times and the bytes moved per step each way."""
+    and ccs_get_state of its result (device -> pinned host).  The host fields of a
+    state are slices of one page-locked block in the order the lane moves them
+    (phi, u, v up; the eight output fields down), so each direction is one copy.
+    Three loops: the async entry points (upload of step k+1 and download of result k
+    overlap the steps; two result buffers in turn), the same with every field in its
+    own pinned array (eleven copies per step), and the synchronous calls one after
+    another.  Returns the three loops' wall times and the bytes moved per step each
+    way."""
     from conformal_cubed_sphere_gb300 import model as M
-    pin_in = {k: torch.from_numpy(state[k].copy()).pin_memory() for k in M.STATE_FIELDS}
-    sin = M.State({k: v.numpy() for k, v in pin_in.items()})
-    outs = []
-    for _ in range(2):
-        pin_out = {k: torch.empty(mesh.ncell, dtype=torch.float64).pin_memory() for k in M.STATE_FIELDS}
-        outs.append(M.State({k: v.numpy() for k, v in pin_out.items()}))
+    sin = pinned_state(M, mesh, torch, ("phi", "u", "v"), fill=state)
+    outs = [pinned_state(M, mesh, torch, M.STATE_FIELDS) for _ in range(2)]
+    sep_in = M.State({k: torch.from_numpy(state[k].copy()).pin_memory().numpy() for k in M.STATE_FIELDS})
+    sep_outs = [M.State({k: torch.empty(mesh.ncell, dtype=torch.float64).pin_memory().numpy()
+                         for k in M.STATE_FIELDS}) for _ in range(2)]
     # inputs the lane uploads / outputs it downloads
     lane_mixed = stepper._cfg.precision == 1
     n_in = 3 if lane_mixed else 8
     n_out = 8
-    cells = 6 * mesh.N * mesh.N
-    for _ in range(2):  # warm-up of both paths
-        stepper.set_state_async(sin)
-        stepper.step_async(1)
-        stepper.get_state_async(outs[0])
-    stepper.sync()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(steps):
-        stepper.set_state_async(sin)
-        stepper.step_async(1)
-        stepper.get_state_async(outs[k % 2])
-    stepper.sync()
-    el_async = time.perf_counter() - t0
+
+    def run_async(si, so):
+        for _ in range(2):  # warm-up
+            stepper.set_state_async(si)
+            stepper.step_async(1)
+            stepper.get_state_async(so[0])
+        stepper.sync()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(steps):
+            stepper.set_state_async(si)
+            stepper.step_async(1)
+            stepper.get_state_async(so[k % 2])
+        stepper.sync()
+        return time.perf_counter() - t0
+
+    el_async = run_async(sin, outs)
+    el_sep = run_async(sep_in, sep_outs)
     t0 = time.perf_counter()
     for _ in range(steps):
         stepper.set_state(sin)
@@ -197,7 +217,7 @@ def e2e_rate(stepper, mesh, state, steps: int, torch):
         stepper.get_state(outs[0])
     el_sync = time.perf_counter() - t0
     nb = mesh.ncell * 8
-    return el_async, el_sync, n_in * nb, n_out * nb
+    return el_async, el_sep, el_sync, n_in * nb, n_out * nb
 
 
 def cpu_baseline(mesh, state, dt, seconds=10.0):
@@ -438,15 +458,16 @@ def main():
     avg64_ms, _ = kernel_launch_avg_ms(f64, 1)
 
     # end to end through the C ABI
-    e2e_steps = max(3, min(20, args.steps))
+    e2e_steps = max(3, min(50, args.steps))
     mixed2 = M.Stepper(mesh, dt, precision="mixed", device=local, phi_mean=phibar)
     mixed2.set_state(s)
     mixed2.set_variant(mixed.variant[0])
     if ws > 1:
         torch.distributed.barrier()
-    el_async, el_sync, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
+    el_async, el_sep, el_sync, h2d, d2h = e2e_rate(mixed2, mesh, s, e2e_steps, torch)
     # every rank moves its own replica's data over its own host link: whole-job rate
     e2e = ws * cells * e2e_steps / slowest_rank_seconds(el_async)
+    e2e_sep = ws * cells * e2e_steps / slowest_rank_seconds(el_sep)
     e2e_sync = ws * cells * e2e_steps / slowest_rank_seconds(el_sync)
 
     if rank != 0:
@@ -467,9 +488,9 @@ def main():
                      "traffic": traffic, "kernel": "mixed_stage_kernel", "kernel_ms_avg": avg_ms,
                      "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "how": "ccs_set_state_async + ccs_step_async(1) + ccs_get_state_async per step, pinned host "
-                       "buffers, one ccs_sync at the end",
-                "synchronous_calls": e2e_sync},
+                "how": "ccs_set_state_async + ccs_step_async(1) + ccs_get_state_async per step, each state's "
+                       "fields in one pinned host block (one copy per direction), one ccs_sync at the end",
+                "separate_field_arrays": e2e_sep, "synchronous_calls": e2e_sync},
         "gpu_launches": 4 * args.steps,
         "clocks": sampler.summary(),
         "cpu_baseline": cpu,

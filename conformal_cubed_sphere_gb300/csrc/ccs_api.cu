@@ -935,6 +935,30 @@ static void mixed_handle_destroy(ccs_handle *h) {
   h->mixed = nullptr;
 }
 
+// Copies n fields of `bytes` each (dst[q] <- src[q], NULL entries skipped), one
+// cudaMemcpyAsync per run of fields whose destination and source both continue the
+// previous field's: a caller whose host arrays are consecutive slices of one
+// page-locked block gets one copy per direction, which the host link overlaps
+// with the other direction better than many smaller copies.
+static cudaError_t copy_field_runs(void *const *dst, const void *const *src, int n, size_t bytes,
+                                   cudaMemcpyKind kind, cudaStream_t s) {
+  int q = 0;
+  while (q < n) {
+    if (!dst[q] || !src[q]) {
+      q++;
+      continue;
+    }
+    int e = q + 1;
+    while (e < n && dst[e] && src[e] && (char *)dst[e] == (char *)dst[e - 1] + bytes &&
+           (const char *)src[e] == (const char *)src[e - 1] + bytes)
+      e++;
+    const cudaError_t err = cudaMemcpyAsync(dst[q], src[q], (size_t)(e - q) * bytes, kind, s);
+    if (err != cudaSuccess) return err;
+    q = e;
+  }
+  return cudaSuccess;
+}
+
 static int mixed_set_state(ccs_handle *h, const ccs_state_view *s, bool sync) {
   MixedLane *M = h->mixed;
   const Layout &L = h->L;
@@ -959,9 +983,9 @@ static int mixed_set_state(ccs_handle *h, const ccs_state_view *s, bool sync) {
   M->in_slot ^= 1;
   double *st = M->stage_in[k];
   CCS_TRY(h, cudaStreamWaitEvent(M->cin, M->in_free[k], 0));
-  CCS_TRY(h, cudaMemcpyAsync(st, s->phi, nref * sizeof(double), cudaMemcpyHostToDevice, M->cin));
-  CCS_TRY(h, cudaMemcpyAsync(st + nref, s->u, nref * sizeof(double), cudaMemcpyHostToDevice, M->cin));
-  CCS_TRY(h, cudaMemcpyAsync(st + 2 * nref, s->v, nref * sizeof(double), cudaMemcpyHostToDevice, M->cin));
+  void *const dst[3] = {st, st + nref, st + 2 * nref};
+  const void *const src[3] = {s->phi, s->u, s->v};
+  CCS_TRY(h, copy_field_runs(dst, src, 3, nref * sizeof(double), cudaMemcpyHostToDevice, M->cin));
   CCS_TRY(h, cudaEventRecord(M->in_ready[k], M->cin));
   CCS_TRY(h, cudaStreamWaitEvent(h->stream, M->in_ready[k], 0));
   const double a2 = h->cfg.radius * h->cfg.radius;
@@ -988,10 +1012,9 @@ static int mixed_get_state(ccs_handle *h, ccs_state_view *s, bool sync) {
                                  h->stream));
   CCS_TRY(h, cudaEventRecord(M->out_ready[k], h->stream));
   CCS_TRY(h, cudaStreamWaitEvent(M->cout, M->out_ready[k], 0));
-  double *dst[8] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC, s->zonal_wind, s->meridional_wind};
-  for (int q = 0; q < 8; q++)
-    if (dst[q])
-      CCS_TRY(h, cudaMemcpyAsync(dst[q], out[q], nref * sizeof(double), cudaMemcpyDeviceToHost, M->cout));
+  void *const dst[8] = {s->phiG, s->u, s->v, s->phi, s->uC, s->vC, s->zonal_wind, s->meridional_wind};
+  const void *const src[8] = {out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7]};
+  CCS_TRY(h, copy_field_runs(dst, src, 8, nref * sizeof(double), cudaMemcpyDeviceToHost, M->cout));
   CCS_TRY(h, cudaEventRecord(M->out_free[k], M->cout));
   if (sync) CCS_TRY(h, cudaStreamSynchronize(M->cout));
   return CCS_OK;

@@ -157,7 +157,11 @@ int ccs_sync(ccs_handle *h);
  * the copies run on two copy streams with double-buffered device staging, so a loop
  * of set_async / step_async / get_async overlaps the upload of one state and the
  * download of the previous result with the step in between; pass page-locked host
- * arrays for the copies to be asynchronous.  No counterpart in the reference. */
+ * arrays for the copies to be asynchronous.  Fields whose host arrays are
+ * consecutive slices of one block (each nh*nh*6 doubles, in the order phi, u, v for
+ * set and phiG, u, v, phi, uC, vC, zonal_wind, meridional_wind for get) move in one
+ * copy per run; the host link overlaps one large upload and one large download
+ * better than many smaller copies.  No counterpart in the reference. */
 int ccs_set_state_async(ccs_handle *h, const ccs_state_view *s);
 int ccs_get_state_async(ccs_handle *h, ccs_state_view *s);
 
