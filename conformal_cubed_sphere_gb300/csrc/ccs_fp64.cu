@@ -418,11 +418,9 @@ int f64_grid_for(int device) {
 template <class T>
 cudaError_t f64_launch(const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
   constexpr int smem = f64_smem_bytes<T>();
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(f64_stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  const cudaError_t e = smem_attr_once((const void *)f64_stage_kernel<T>, smem, attr_done);
+  if (e != cudaSuccess) return e;
   if (grid > nwork) grid = nwork;
   if (grid < 1) return cudaSuccess;
   f64_stage_kernel<T><<<grid, NT, smem, s>>>(d_stages, d_work, nwork);

@@ -3,9 +3,27 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <cstdint>
+
 #include "ccs_internal.h"
 
 namespace ccs {
+
+// Raises a kernel's dynamic shared-memory limit once per device: the attribute is
+// held per device, so a process driving handles on several devices sets it on each
+// (`done` is the kernel's own set of device bits; ordinals above 63 set it every
+// launch).
+inline cudaError_t smem_attr_once(const void *fn, int smem, std::atomic<uint64_t> &done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = dev >= 0 && dev < 64 ? (uint64_t)1 << dev : 0;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 // One tile of work: instance, panel (0..5) and tile coordinates.
 struct WorkItem {

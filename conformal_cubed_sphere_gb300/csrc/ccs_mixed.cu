@@ -686,12 +686,9 @@ int mx_grid_for(int device) {  // the WENO instance bounds the occupancy of all
 template <class T, bool CENTRAL, bool EDISS>
 cudaError_t mx_launch(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
   constexpr int smem = (int)sizeof(SmemMx<T>);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(mixed_stage_kernel<T, CENTRAL, EDISS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         smem);
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  const cudaError_t e = smem_attr_once((const void *)mixed_stage_kernel<T, CENTRAL, EDISS>, smem, attr_done);
+  if (e != cudaSuccess) return e;
   if (grid > nwork) grid = nwork;
   if (grid < 1) return cudaSuccess;
   mixed_stage_kernel<T, CENTRAL, EDISS><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
