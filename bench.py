@@ -14,7 +14,8 @@ FP32/FP64 lane; the FP64 parity lane is measured beside it on the same state.
              pinned host), one ccs_sync at the end, so one step's copies overlap
              the neighbouring steps; the synchronous calls are reported beside it
   roofline   the mixed stage kernel's average launch duration against the
-             measured HBM copy bandwidth
+             measured HBM copy bandwidth; roofline.issue puts the same launches
+             against the bound the kernel actually has, instruction issue
   cpu_baseline  the CPU FP64 oracle (a restatement of the reference step) on the
              host cores, on a bounded sample of the workload
 
@@ -124,6 +125,20 @@ def _traffic_per_launch(name: str):
         return d.get(name)
     except Exception:
         return None
+
+
+def issue_roofline(avg_ms, warp_inst, sms, clocks):
+    """The stage kernel against its actual bound, instruction issue: warp instructions
+    per launch (ncu, committed summary) over the launch time, against one warp
+    instruction per cycle on each of the four schedulers of every SM at the SM clock
+    sampled during the timed region."""
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if not warp_inst or not mhz:
+        return None
+    achieved = warp_inst / (avg_ms * 1e-3)
+    peak = 4 * sms * mhz * 1e6
+    return {"achieved": achieved, "peak": peak, "unit": "warp inst/s", "frac": achieved / peak,
+            "warp_inst_per_launch": warp_inst}
 
 
 def build_case(N=N_BENCH, seed=SEED, oro=True):
@@ -472,6 +487,7 @@ def main():
 
     if rank != 0:
         return
+    clocks = sampler.summary()
     cpu = None if args.no_cpu else cpu_baseline(mesh, s, dt)
     line = {
         "metric": "C384 cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": ws,
@@ -486,13 +502,17 @@ def main():
                       "kernel_ms_avg": avg64_ms, "mixed_over_fp64": value / ws / fp64_value},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": "mixed_stage_kernel", "kernel_ms_avg": avg_ms,
-                     "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind},
+                     "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind,
+                     "issue": issue_roofline(avg_ms, _traffic_per_launch(f"mixed_stage_C{mesh.N}_warp_inst")
+                                             if mixed.variant[0] == 0 else None,  # the profiled 32x32 tile
+                                             torch.cuda.get_device_properties(local).multi_processor_count,
+                                             clocks)},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "how": "ccs_set_state_async + ccs_step_async(1) + ccs_get_state_async per step, each state's "
                        "fields in one pinned host block (one copy per direction), one ccs_sync at the end",
                 "separate_field_arrays": e2e_sep, "synchronous_calls": e2e_sync},
         "gpu_launches": 4 * args.steps,
-        "clocks": sampler.summary(),
+        "clocks": clocks,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
