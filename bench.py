@@ -127,6 +127,20 @@ def _traffic_per_launch(name: str):
         return None
 
 
+def fp64_roofline(avg_ms, fp64_inst, sms, clocks):
+    """The FP64 lane's stage kernel against its bound, the FP64 pipe: FP64 thread
+    instructions per launch (ncu, committed summary) over the launch time, against
+    two FP64 lanes per SM per cycle at the SM clock sampled during the timed region
+    (DFMA counted once; 1.26 TFLOP/s counting it as two flops at 2070 MHz)."""
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if not fp64_inst or not mhz:
+        return None
+    achieved = fp64_inst / (avg_ms * 1e-3)
+    peak = 2 * sms * mhz * 1e6
+    return {"bound": "fp64 pipe", "achieved": achieved, "peak": peak, "unit": "FP64 thread inst/s",
+            "frac": achieved / peak, "fp64_inst_per_launch": fp64_inst}
+
+
 def issue_roofline(avg_ms, warp_inst, sms, clocks):
     """The stage kernel against its actual bound, instruction issue: warp instructions
     per launch (ncu, committed summary) over the launch time, against one warp
@@ -499,7 +513,11 @@ def main():
                    "parallelism": "replicas" if ws > 1 else "single",
                    "tile_variants": {lane: {"chosen": v, "launch_us": t} for lane, (v, t) in tuned.items()}},
         "fp64_lane": {"value": fp64_value, "unit": "cell-steps/s", "ms_per_step": 1e3 * t_f64 / args.fp64_steps,
-                      "kernel_ms_avg": avg64_ms, "mixed_over_fp64": value / ws / fp64_value},
+                      "kernel_ms_avg": avg64_ms, "mixed_over_fp64": value / ws / fp64_value,
+                      "roofline": fp64_roofline(avg64_ms, _traffic_per_launch(f"f64_stage_C{mesh.N}_fp64_thread_inst")
+                                                if f64.variant[0] == 1 else None,  # the profiled 16x16 tile
+                                                torch.cuda.get_device_properties(local).multi_processor_count,
+                                                clocks)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": "mixed_stage_kernel", "kernel_ms_avg": avg_ms,
                      "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind,

@@ -39,3 +39,12 @@ def test_issue_roofline():
     assert r["frac"] == pytest.approx(r["achieved"] / r["peak"])
     assert bench.issue_roofline(0.05, None, 152, {"sm_mhz": 2000.0}) is None
     assert bench.issue_roofline(0.05, 3.0e7, 152, {"sm_mhz": None, "sm_max_mhz": None}) is None
+
+
+def test_fp64_roofline():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    r = bench.fp64_roofline(3.5, 1.9e9, 152, {"sm_mhz": 2070.0})
+    assert r["peak"] == pytest.approx(2 * 152 * 2070e6)
+    assert r["frac"] == pytest.approx(1.9e9 / 3.5e-3 / (2 * 152 * 2070e6))
+    assert bench.fp64_roofline(3.5, None, 152, {"sm_mhz": 2070.0}) is None
