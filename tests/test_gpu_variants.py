@@ -120,3 +120,27 @@ def test_batch_groups_mixed_members_by_operator():
         a, b = x.get_state(), r.get_state()
         for k in CHECK_FIELDS:
             assert bitwise_equal(a[k], b[k], m), (op, k)
+
+
+def test_batch_members_with_different_halos():
+    """One launch per group over members whose arrays have different halo widths
+    (3, 4, 5; FP64 and mixed): each member's layout travels in its own stage
+    descriptor, and every member equals its single run bit for bit."""
+    members, refs = [], []
+    for k, (N, halo, lane) in enumerate([(16, 3, "fp64"), (16, 5, "fp64"), (20, 4, "fp64"),
+                                         (16, 3, "mixed"), (20, 4, "mixed"), (24, 5, "mixed")]):
+        mesh, s, dt = seeded_case(N, halo, seed=60 + k, oro=True)
+        kw = dict(phi_mean=8000.0 * mesh.gravity) if lane == "mixed" else {}
+        x = M.Stepper(mesh, dt, precision=lane, **kw)
+        x.set_state(s)
+        r = M.Stepper(mesh, dt, precision=lane, **kw)
+        r.set_state(s)
+        members.append(x)
+        refs.append(r)
+    M.Batch(members).step(3)
+    for x, r in zip(members, refs):
+        r.step(3)
+        a, b = x.get_state(), r.get_state()
+        m = valid_mask(x.mesh)
+        for k in CHECK_FIELDS:
+            assert bitwise_equal(a[k], b[k], m), (x.mesh.N, x.mesh.halo, k)
