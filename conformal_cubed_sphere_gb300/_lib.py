@@ -1,14 +1,17 @@
 """ctypes binding of the C ABI declared in include/ccs_gpu.h.
 
 The library is the in-tree ``_build/libccs_gpu.so``; importing this module fails
-loudly when it has not been built (there is no CPU fallback for the step).
+loudly when it has not been built (there is no CPU fallback for the step).  The
+environment variable CCS_GPU_LIB selects another in-tree build of the same ABI (the
+bounds-checked ``_build/bounds/libccs_gpu.so``) for a whole process.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "_build" / "libccs_gpu.so"
+LIB_PATH = Path(os.environ.get("CCS_GPU_LIB") or Path(__file__).resolve().parent / "_build" / "libccs_gpu.so")
 
 CCS_OK = 0
 CCS_ERR_ARG = 1
@@ -102,6 +105,8 @@ SIGNATURES = {
     "ccs_timing": (C.c_int, [_vp, C.c_int, C.c_int, _dp, C.POINTER(C.c_int64)]),
     "ccs_stream": (C.c_void_p, [_vp]),
     "ccs_selftest_div": (C.c_int, [_dp, C.c_int64, C.c_double, _dp, _dp]),
+    "ccs_debug_bounds": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
+    "ccs_debug_bounds_selftest": (C.c_int, []),
     "ccs_strerror": (C.c_char_p, [C.c_int]),
     "ccs_mesh_save": (C.c_int, [C.c_char_p, C.c_int, C.c_int] + [_dp] * 6),
     "ccs_mesh_file_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),

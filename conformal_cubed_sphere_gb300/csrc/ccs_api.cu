@@ -727,7 +727,7 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
   // shared: s inv_s lamx lamy (one panel each; the face metrics followed by 32 zero
   // rows that the stage kernel's one-face-ahead prefetch may read in partial tiles)
   // + ig as float4; per panel: phis fs
-  const size_t pad = 32 * (size_t)L.pitch;  // a multiple of 4 floats: ig stays 16-byte aligned
+  const size_t pad = kLamPadRows * (size_t)L.pitch;  // a multiple of 4 floats: ig stays 16-byte aligned
   const size_t o_lamx = 2 * np, o_lamy = 3 * np + pad, o_ig = 4 * np + 2 * pad;
   const size_t nfloat = o_ig + 4 * np + 2 * nf;  // s, inv_s, lamx, lamy, ig (4 per cell), phis, fs
   CCS_TRY(h, cudaMalloc(&dm->buf32, nfloat * sizeof(float)));
@@ -1323,6 +1323,44 @@ static int batch_enqueue(ccs_batch *b, bool with_sw) {
     if (cudaStreamWaitEvent(b->stream, g.done, 0) != cudaSuccess) return CCS_ERR_CUDA;
   }
   return CCS_OK;
+}
+
+extern "C" int ccs_debug_bounds(int *site, int64_t *index) {
+  if (!site || !index) return CCS_ERR_ARG;
+#ifndef CCS_BOUNDS
+  *site = -1;
+  *index = 0;
+  return CCS_OK;
+#else
+  if (cudaDeviceSynchronize() != cudaSuccess) return CCS_ERR_CUDA;
+  const unsigned long long a = f64_bounds_take(), b = mixed_bounds_take();
+  const unsigned long long v = a ? a : b;
+  *site = (int)(v >> 48);
+  long long i = (long long)(v & 0xffffffffffffull);
+  if (i & (1ll << 47)) i -= 1ll << 48;  // the index's sign
+  *index = *site ? i : 0;
+  return CCS_OK;
+#endif
+}
+
+extern "C" int ccs_debug_bounds_selftest(void) {
+#ifndef CCS_BOUNDS
+  return CCS_ERR_UNSUPPORTED;
+#else
+  int site = 0;
+  int64_t idx = 0;
+  int rc = ccs_debug_bounds(&site, &idx);  // start clean
+  if (rc) return rc;
+  if (launch_bounds_selftest(7, 3, 999, 0) != cudaSuccess) return CCS_ERR_CUDA;
+  if (launch_bounds_selftest(-2, 3, 998, 0) != cudaSuccess) return CCS_ERR_CUDA;  // the first hit stays
+  if (launch_bounds_selftest(1, 3, 997, 0) != cudaSuccess) return CCS_ERR_CUDA;   // in range: no hit
+  rc = ccs_debug_bounds(&site, &idx);
+  if (rc) return rc;
+  if (site != 999 || idx != 7) return CCS_ERR_CUDA;
+  rc = ccs_debug_bounds(&site, &idx);
+  if (rc) return rc;
+  return site == 0 ? CCS_OK : CCS_ERR_CUDA;
+#endif
 }
 
 extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out) {

@@ -18,6 +18,7 @@
 // own metric.  The output slot never feeds the same launch, so one launch per
 // stage is the whole grid-wide dependency.
 #include "ccs_kernels.h"
+#include "ccs_bounds.cuh"
 
 namespace ccs {
 
@@ -156,8 +157,8 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
       const int i = i0 - 3 + li, j = j0 - 3 + lj;
       double phit = 0., phitG = 0., E = 0., Fx = 0., Fy = 0., uC = 0., vC = 0., g11 = 0., g22 = 0., u = 0.,
              v = 0.;
-      if (i >= -2 && i <= N + 3 && j >= -2 && j <= N + 3 && !is_corner(i, j, N)) {
-        const int64_t c = L.idx(i, j, p);
+      const int64_t c = L.idx(i, j, p);
+      if (i >= -2 && i <= N + 3 && j >= -2 && j <= N + 3 && !is_corner(i, j, N) && ccs_inb(c, L.field, 201)) {
         const double phiG = st.in.phiG[c], phi = st.in.phi[c];
         u = st.in.u[c];
         v = st.in.v[c];
@@ -187,7 +188,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
       if (face < NFX) {
         const int fi = face % (TX + 1), lj = face / (TX + 1);
         const int f = i0 - 1 + fi, j = j0 + lj;
-        if (j <= N && f <= N) {
+        if (j <= N && f <= N && ccs_inb((lj + 3) * RX + fi + 5, RN, 211)) {
           fld = (q < 2) ? S.Fx : (q < 4) ? S.E : (q < 6) ? S.phitG : S.u;
           const double *row = fld + (lj + 3) * RX;
           if ((q & 1) == 0)  // "+" from cell f: field(f-2 .. f+2)
@@ -199,7 +200,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
         const int fy = face - NFX;
         const int li = fy % TX, fj = fy / TX;
         const int g = j0 - 1 + fj, i = i0 + li;
-        if (i <= N && g <= N) {
+        if (i <= N && g <= N && ccs_inb(li + 3 + (fj + 5) * RX, RN, 212)) {
           fld = (q < 2) ? S.Fy : (q < 4) ? S.E : (q < 6) ? S.phitG : S.v;
           const double *col = fld + (li + 3);
           if ((q & 1) == 0)
@@ -210,7 +211,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
                              col[(fj + 5) * RX]);
         }
       }
-      rec[q * NF + face] = val;
+      if (ccs_inb(q * NF + face, 8 * NF, 213)) rec[q * NF + face] = val;
     }
     __syncthreads();
 
@@ -228,6 +229,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
       if (face < NFX) {
         const int fi = face % (TX + 1), lj = face / (TX + 1);
         const int r = (lj + 3) * RX + fi + 2;  // cell f; cell f+1 is r + 1
+        if (!ccs_inb(r + 1, RN, 214)) continue;
         a = S.uC[r + 1]; b = S.uC[r];
         ga = S.ig11[r + 1]; gb = S.ig11[r];
         pa = S.phit[r + 1]; pb = S.phit[r];
@@ -235,6 +237,7 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
         const int fy = face - NFX;
         const int li = fy % TX, fj = fy / TX;
         const int r = (fj + 2) * RX + li + 3;  // cell g; cell g+1 is r + RX
+        if (!ccs_inb(r + RX, RN, 215)) continue;
         a = S.vC[r + RX]; b = S.vC[r];
         ga = S.ig22[r + RX]; gb = S.ig22[r];
         pa = S.phit[r + RX]; pb = S.phit[r];
@@ -254,9 +257,10 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
     {
       const int li = tid % TX, lj = tid / TX;
       const int i = i0 + li, j = j0 + lj;
-      if (i <= N && j <= N) {
-        const int64_t c = L.idx(i, j, p);
-        const int rc = (lj + 3) * RX + li + 3;
+      const int64_t c = L.idx(i, j, p);
+      const int rc = (lj + 3) * RX + li + 3;
+      if (i <= N && j <= N && ccs_inb(c, L.field, 221) && ccs_inb(rc + 3 * RX, RN, 222) &&
+          ccs_inb(NFX + (lj + 1) * TX + li, NF, 223)) {
         double dfluxdx, dEdx, dvdx, dfluxdy, dEdy, dudy;
         if (op == CCS_OP_WENO) {
           const double *FF = rec, *EF = rec + NF;
@@ -356,7 +360,10 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
             else if (side == 2) { k = j; m = i; }
             else { k = N + 1 - j; m = i; }
             if (k > h) continue;
-            const int64_t d = st.m.push[((int64_t)p * 4 + side) * h * N + (int64_t)(k - 1) * N + (m - 1)];
+            const int64_t e = ((int64_t)p * 4 + side) * h * N + (int64_t)(k - 1) * N + (m - 1);
+            if (!ccs_inb(e, (long long)24 * h * N, 224)) continue;
+            const int64_t d = st.m.push[e];
+            if (!ccs_inb(d, L.field, 225)) continue;
             const double ud = st.m.gia11[d] * zon + st.m.gia12[d] * mer;
             const double vd = st.m.gia21[d] * zon + st.m.gia22[d] * mer;
             st.out.phiG[d] = np;
@@ -387,6 +394,8 @@ __global__ void div_const_check_kernel(const double *__restrict__ x, int64_t n, 
     out[n + k] = x[k] / b;
   }
 }
+
+unsigned long long f64_bounds_take() { return bounds_take_tu(); }
 
 cudaError_t launch_div_const_check(const double *x, int64_t n, double b, double *out, cudaStream_t s) {
   div_const_check_kernel<<<1024, 256, 0, s>>>(x, n, b, 1. / b, out);

@@ -116,6 +116,19 @@ cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp,
 // test support: correctly rounded division by a constant, see ccs_fp64.cu
 cudaError_t launch_div_const_check(const double *x, int64_t n, double b, double *out, cudaStream_t s);
 
+// Bounds-checked build (-DCCS_BOUNDS, ccs_bounds.cuh): the first out-of-range index
+// the FP64 / mixed kernels met since the last call, (site << 48) | (index & 2^48-1),
+// 0 for none; the call clears it.  Always 0 in the normal build.
+unsigned long long f64_bounds_take();
+unsigned long long mixed_bounds_take();
+// one thread checks index i against [0, n) under `site`, accessing nothing (a no-op
+// in the normal build)
+cudaError_t launch_bounds_selftest(long long i, long long n, int site, cudaStream_t s);
+
+// zero rows after each face wave-speed metric block of the mixed lane (the line
+// sweep fetches one face ahead and reads faces past N in partial tiles)
+constexpr int kLamPadRows = 32;
+
 // FP64 reductions (mass / energy) over the interior of an FP64 state
 cudaError_t launch_f64_diag(const Layout &L, const double *phiG, const double *phi, const double *u,
                             const double *v, const double *uC, const double *vC, const double *sqrtG,

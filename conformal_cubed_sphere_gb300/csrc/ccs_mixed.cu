@@ -16,6 +16,7 @@
 // before rounding instead of after; the weights are the reference's WENO-Z
 // weights with eps rescaled to the non-dimensional fields.
 #include "ccs_kernels.h"
+#include "ccs_bounds.cuh"
 
 namespace ccs {
 
@@ -211,6 +212,7 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
   const int stp = XDIR ? 1 : SP;
   const int base = XDIR ? (line + 3) * SP + 2 : 2 * SP + line + 3;  // cell ci = 0 of the line
   int o = base + (f0 - 2) * stp;
+  if (!ccs_inb(o, T::RN, 111) || !ccs_inb(o + 3 * stp, T::RN, 112)) return;
   // window values at cells c-2 .. c+1 for c = f0
   float Fv[4], Ev[4], hv[4], sv[4];
 #pragma unroll
@@ -239,15 +241,17 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
   // the 32 padding rows the metric arrays carry after each panel block
   const float *lp = lam + (XDIR ? L.idx(startg + f0, lineg, 0) : L.idx(lineg, startg + f0, 0));
   const int lstride = XDIR ? 1 : L.pitch;
-  float lam_next = __ldg(lp);
+  const long long lam_n = L.panel + (long long)kLamPadRows * L.pitch;  // face-metric block + padding
+  float lam_next = ccs_inb(lp - lam, lam_n, 115) ? __ldg(lp) : 0.f;
   for (int k = 0; k <= NFACE; k++) {
     const int ci = f0 + k;
     const float lam_cur = lam_next;
     if (k > 0 && k < NFACE) {
       lp += lstride;
-      lam_next = __ldg(lp);
+      lam_next = ccs_inb(lp - lam, lam_n, 115) ? __ldg(lp) : 0.f;
     }
     const int on = base + (ci + 2) * stp;  // cell c+2
+    if (!ccs_inb(on, T::RN, 113) || !ccs_inb(base + ci * stp, T::RN, 114)) break;
     const float Fn = Qflux[on], En = S.E[on], hn = S.hs[on], sn = S.s[on];
     const float qn = hn * sn;
     const float dF3 = Fn - Flast, dE3 = En - Elast, dP3 = fmaf(phibar, sn - slast, qn - qlast);
@@ -282,9 +286,11 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
         const float gE = EDISS ? 0.5f * fmaf(-lm * st.a2, dU1 + DUm - pDUp, dE1 + pDEp + DEm)
                                : 0.5f * (dE1 + pDEp + DEm);
         if (XDIR) {
-          S.gx[0][line][fi] = gF;
-          S.gx[1][line][fi] = gE;
-        } else {
+          if (ccs_inb((long long)line * T::NFL + fi, (long long)T::TY * T::NFL, 116)) {
+            S.gx[0][line][fi] = gF;
+            S.gx[1][line][fi] = gE;
+          }
+        } else if (ccs_inb((long long)fi * T::TX + line, (long long)(T::TY + 1) * T::TX, 117)) {
           S.gy[0][fi][line] = gF;
           S.gy[1][fi][line] = gE;
         }
@@ -348,8 +354,9 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         const int li = r % RX, lj = r / RX;
         const int i = i0 - 3 + li, j = j0 - 3 + lj;
         float F = 0.f, G = 0.f, E = 0.f, hs = 0.f, sc = 1.f, uC = 0.f, vC = 0.f, u = 0.f, v = 0.f;
-        if (i <= N + 3 && j <= N + 3 && !corner(i, j, N)) {
-          const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
+        const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
+        if (i <= N + 3 && j <= N + 3 && !corner(i, j, N) && ccs_inb(c, L.field, 101) &&
+            ccs_inb(cs, L.panel, 102)) {
           const float hp = __ldg(ihp + c);
           u = __ldg(iu + c);
           v = __ldg(iv + c);
@@ -364,6 +371,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
           E = fmaf(ha2, fmaf(u, uC, v * vC), hs);  // E - phibar
         }
         const int a = lj * SP + li;
+        if (!ccs_inb(a, T::RN, 103)) continue;
         S.F[a] = F; S.G[a] = G; S.E[a] = E; S.hs[a] = hs; S.s[a] = sc;
         S.uC[a] = uC; S.vC[a] = vC; S.u[a] = u; S.v[a] = v;
       }
@@ -400,6 +408,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       for (int q = 0; q < 3; q++) q_y0[k][q] = q_a[k][q] = q_lo[k][q] = 0.f;
       if (i > N || j > N) continue;
       const int64_t c = L.idx(i, j, p);
+      if (!ccs_inb(c, L.field, 121) || !ccs_inb(L.idx(i, j, 0), L.panel, 122)) continue;
       q_fs[k] = __ldg(st.m.fs + c);
       q_is[k] = __ldg(st.m.inv_s + L.idx(i, j, 0));
       if (kind == K_TEND) continue;
@@ -417,6 +426,11 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       const int i = i0 + li, j = j0 + lj;
       if (i > N || j > N) continue;
       const int r = (lj + 3) * SP + li + 3;
+      if (!ccs_inb(r - 3 * SP, T::RN, 131) || !ccs_inb(r + 3 * SP, T::RN, 132) ||
+          !ccs_inb((long long)lj * T::NFL + li + 1, (long long)T::TY * T::NFL, 133) ||
+          !ccs_inb((long long)(lj + 1) * T::TX + li, (long long)(T::TY + 1) * T::TX, 134) ||
+          !ccs_inb(L.idx(i, j, p), L.field, 135))
+        continue;
       float divx, dEdx, divy, dEdy, dvdx, dudy;
       if (!CENTRAL) {
         divx = (S.gx[0][lj][li + 1] - S.gx[0][lj][li] + (S.F[r] - S.F[r - 1])) * st.rdx;
@@ -538,7 +552,9 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         const int i = sd < 2 ? x : m, j = sd < 2 ? m : x;
         const int64_t c = L.idx(i, j, p);
         const int64_t e = ((int64_t)p * 4 + sd) * h * N + (int64_t)(k - 1) * N + (m - 1);
+        if (!ccs_inb(e, (long long)24 * h * N, 141) || !ccs_inb(c, L.field, 143)) continue;
         const int64_t d = st.m.push[e];
+        if (!ccs_inb(d, L.field, 142)) continue;
         const double *X = st.m.xf + 4 * e;
         const float np = st.out.hp[c], nu = st.out.u[c], nv = st.out.v[c];
         const double ud = fma(X[0], (double)nu, X[1] * (double)nv);
@@ -749,6 +765,18 @@ cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp,
                               int nblocks, cudaStream_t s) {
   mixed_diag_kernel<<<nblocks, 256, 0, s>>>(L, st, lohp, lou, lov, m, phibar, a2, partials);
   return cudaGetLastError();
+}
+
+unsigned long long mixed_bounds_take() { return bounds_take_tu(); }
+
+cudaError_t launch_bounds_selftest(long long i, long long n, int site, cudaStream_t s) {
+#ifdef CCS_BOUNDS
+  bounds_selftest_kernel<<<1, 32, 0, s>>>(i, n, site);
+  return cudaGetLastError();
+#else
+  (void)i; (void)n; (void)site; (void)s;
+  return cudaSuccess;
+#endif
 }
 
 }  // namespace ccs

@@ -250,6 +250,18 @@ int ccs_timing(ccs_handle *h, int enable, int reset, double *kernel_ms, int64_t 
  * device 0 with temporary buffers. */
 int ccs_selftest_div(const double *x, int64_t n, double b, double *fast, double *ieee);
 
+/* Bounds-checked build (libccs_gpu.so built with -DCCS_BOUNDS, build.build_bounds):
+ * the kernels check their array indices and skip, instead of performing, any access
+ * outside its array, recording the first such index.  ccs_debug_bounds waits for
+ * the current device, returns the first recorded check site (0: none) and index
+ * since its last call and clears them; in the normal build it sets *site = -1.
+ * ccs_debug_bounds_selftest checks the recording path with a kernel that tests an
+ * out-of-range index and accesses nothing (CCS_ERR_UNSUPPORTED in the normal
+ * build).  No counterpart in the reference (its DEBUG builds add -fcheck=all,
+ * CMakeLists.txt:9,17). */
+int ccs_debug_bounds(int *site, int64_t *index);
+int ccs_debug_bounds_selftest(void);
+
 /* The CUDA stream (a cudaStream_t) every launch of this handle is ordered on, so
  * that a caller can place its own events or copies before and after a step. */
 void *ccs_stream(ccs_handle *h);
