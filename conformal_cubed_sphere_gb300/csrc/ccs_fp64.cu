@@ -150,6 +150,12 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
     const int i0 = 1 + wi.tx * TX, j0 = 1 + wi.ty * TY;
     const int nrec = st.ediss ? 8 : 6;
     const int op = st.op;  // uniform over the work item
+#ifdef CCS_BOUNDS
+    // poison the tile arrays: a read of a slot this tile never wrote shows up as NaN
+    // in the result (checked build only)
+    for (int k = tid; k < NCELL_ARR * RN + 8 * NF; k += NT) smem_raw[k] = __longlong_as_double(0x7ff8000000000000LL);
+    __syncthreads();
+#endif
 
     // ---- phase 1: cell quantities (spatial_operators_mod.F90:71-78) ----------
     for (int r = tid; r < RN; r += NT) {

@@ -337,6 +337,14 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
       const int *src = reinterpret_cast<const int *>(stages + wi.inst);
       int *dst = reinterpret_cast<int *>(&S.st);
       for (int k = tid; k < nw; k += NT) dst[k] = src[k];
+#ifdef CCS_BOUNDS
+      // poison the tile arrays: a read of a slot this tile never wrote shows up as
+      // NaN in the result (checked build only)
+      float *a = S.F;
+      const int na = (int)((reinterpret_cast<const char *>(&S.gy[1][T::TY][T::TX - 1]) + sizeof(float) -
+                            reinterpret_cast<const char *>(S.F)) / sizeof(float));
+      for (int k = tid; k < na; k += NT) a[k] = __int_as_float(0x7fc00000);
+#endif
     }
     __syncthreads();
     const MixedStage &st = S.st;

@@ -1,7 +1,9 @@
 """Small cases run in a process that loaded the bounds-checked library (CCS_GPU_LIB):
 both lanes, every tile variant, partial tiles, halos from 3 to the panel width, both
 RK schemes, the E-flux options, the central operators, the tendency entry point,
-transfers and a batch.  Exits non-zero at the first recorded out-of-range index.
+transfers and a batch.  Exits non-zero at the first recorded out-of-range index or
+at a state that the health check rejects (the checked build poisons each tile's
+shared arrays with NaN, so a read of a never-written slot would show there).
 The FP64 results are also checked bit for bit against the oracle on one case, so
 the checked build is known to compute what the normal build computes."""
 import ctypes as C
@@ -24,6 +26,14 @@ def hits(tag):
     L.check(L.lib().ccs_debug_bounds(C.byref(site), C.byref(idx)), "ccs_debug_bounds")
     if site.value != 0:
         raise SystemExit(f"{tag}: out-of-range index {idx.value} at check site {site.value}")
+
+
+def healthy(stepper, tag):
+    """The checked build fills each tile's shared arrays with NaN before use, so a
+    read of a slot the tile never wrote would reach the state as NaN."""
+    nbad = stepper.check_state()
+    if nbad:
+        raise SystemExit(f"{tag}: {nbad} cells non-finite or of non-positive depth")
 
 
 def main():
@@ -50,6 +60,7 @@ def main():
                 g.spatial_operator()
                 g.get_state()
                 hits(f"fp64 C{N} h{halo} tile {var} {scheme} ediss {ediss}")
+                healthy(g, f"fp64 C{N} h{halo} tile {var} {scheme} ediss {ediss}")
         for var in (0, 1):
             for scheme, ediss, op in (("RK4", 0, L.CCS_OP_WENO), ("RK3_TVD", 1, L.CCS_OP_WENO),
                                       ("RK4", 0, L.CCS_OP_CENTRAL4)):
@@ -58,10 +69,10 @@ def main():
                 g.set_state(s)
                 g.step(2)
                 g.spatial_operator()
-                g.check_state()
                 g.get_state()
                 g.diag()
                 hits(f"mixed C{N} h{halo} tile {var} {scheme} ediss {ediss} op {op}")
+                healthy(g, f"mixed C{N} h{halo} tile {var} {scheme} ediss {ediss} op {op}")
     # a batch over both lanes and several halo widths
     members = []
     for k, (N, halo, lane) in enumerate([(8, 3, "fp64"), (20, 4, "mixed"), (6, 6, "mixed"), (4, 4, "fp64")]):
@@ -71,6 +82,8 @@ def main():
         members.append(x)
     M.Batch(members).step(2)
     hits("batch")
+    for x in members:
+        healthy(x, "batch")
     # the checked build computes what the normal build does: FP64 bitwise with the oracle
     mesh, s, dt = seeded_case(20, 4, seed=3)
     g = M.Stepper(mesh, dt, precision="fp64")
