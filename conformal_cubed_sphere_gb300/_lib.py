@@ -106,6 +106,7 @@ SIGNATURES = {
     "ccs_stream": (C.c_void_p, [_vp]),
     "ccs_selftest_div": (C.c_int, [_dp, C.c_int64, C.c_double, _dp, _dp]),
     "ccs_debug_bounds": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
+    "ccs_courant": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ccs_debug_bounds_selftest": (C.c_int, []),
     "ccs_strerror": (C.c_char_p, [C.c_int]),
     "ccs_mesh_save": (C.c_int, [C.c_char_p, C.c_int, C.c_int] + [_dp] * 6),

@@ -51,6 +51,47 @@ __global__ void health_kernel(Layout L, const R *__restrict__ hp, const R *__res
   }
 }
 
+// Largest wave speed of a state over interior and edge-halo cells (the cells of
+// ccs_cfl_dt): max(|uC| + sqrt(IG11 phit), |vC| + sqrt(IG22 phit)), phit = phi0 + hp +
+// phis, in FP64; a cell with non-positive phit or a non-finite value counts as +inf.
+// FP64 lane: hp = phi, uC / vC from the state.  Mixed lane: hp = phi - phi0 and the
+// covariant wind / a^2 in FP32, uC / vC formed with the FP64 metric.  The maximum is
+// an atomicMax on the bit patterns (non-negative doubles order as integers).
+__global__ void courant_kernel(Layout L, const float *__restrict__ hp32, const float *__restrict__ u32,
+                               const float *__restrict__ v32, const double *__restrict__ phi64,
+                               const double *__restrict__ uC64, const double *__restrict__ vC64, MeshF64 m,
+                               double phi0, double a2, unsigned long long *lmax) {
+  const int N = L.N, n2 = N + 2;
+  const int64_t ncell = (int64_t)n2 * n2 * 6;
+  double best = 0.;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < ncell;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % n2), j = (int)((q / n2) % n2), p = (int)(q / ((int64_t)n2 * n2));
+    if ((i < 1 || i > N) && (j < 1 || j > N)) continue;  // corner blocks
+    const int64_t c = L.idx(i, j, p);
+    double pt, uC, vC;
+    if (phi64) {
+      pt = phi64[c] + m.phis[c];
+      uC = uC64[c];
+      vC = vC64[c];
+    } else {
+      pt = phi0 + (double)hp32[c] + m.phis[c];
+      const double u = (double)u32[c] * a2, v = (double)v32[c] * a2;
+      uC = m.ig11[c] * u + m.ig12[c] * v;
+      vC = m.ig21[c] * u + m.ig22[c] * v;
+    }
+    double x = INFINITY;
+    if (pt > 0.) {
+      const double lx = fabs(uC) + sqrt(m.ig11[c] * pt), ly = fabs(vC) + sqrt(m.ig22[c] * pt);
+      const double l = fmax(lx, ly);
+      if (l >= 0. && l < INFINITY) x = l;
+    }
+    best = fmax(best, x);
+  }
+  for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(lmax, (unsigned long long)__double_as_longlong(best));
+}
+
 #define CCS_TRY(h, call)                                                       \
   do {                                                                         \
     cudaError_t e_ = (call);                                                   \
@@ -117,6 +158,7 @@ struct ccs_handle {
   // diagnostics
   double *d_partials = nullptr;
   unsigned long long *d_bad = nullptr;  // health-check counter
+  unsigned long long *d_lmax = nullptr;  // largest wave speed (ccs_courant), as bits
   // mixed lane
   struct MixedLane *mixed = nullptr;
 };
@@ -533,6 +575,7 @@ void ccs_destroy(ccs_handle *h) {
   if (h->d_work) cudaFree(h->d_work);
   if (h->d_partials) cudaFree(h->d_partials);
   if (h->d_bad) cudaFree(h->d_bad);
+  if (h->d_lmax) cudaFree(h->d_lmax);
   if (h->mixed) mixed_handle_destroy(h);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1141,6 +1184,33 @@ extern "C" int ccs_check_state(ccs_handle *h, int64_t *bad_cells) {
   CCS_TRY(h, cudaStreamSynchronize(h->stream));
   if (bad_cells) *bad_cells = (int64_t)bad;
   return bad ? CCS_ERR_NAN : CCS_OK;
+}
+
+extern "C" int ccs_courant(ccs_handle *h, double *courant) {
+  if (!h || !courant) return CCS_ERR_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (!h->d_lmax) CCS_TRY(h, cudaMalloc(&h->d_lmax, sizeof(unsigned long long)));
+  CCS_TRY(h, cudaMemsetAsync(h->d_lmax, 0, sizeof(unsigned long long), h->stream));
+  const int64_t ncell = (int64_t)(h->L.N + 2) * (h->L.N + 2) * 6;
+  const int grid = (int)std::min<int64_t>((ncell + 255) / 256, 4096);
+  const MeshF64 &m = h->mesh->m64;
+  if (h->cfg.precision == CCS_MIXED) {
+    MixedLane *M = h->mixed;
+    if (!M->have_phibar) return CCS_ERR_ARG;
+    courant_kernel<<<grid, 256, 0, h->stream>>>(h->L, M->S[0].hp, M->S[0].u, M->S[0].v, nullptr, nullptr, nullptr,
+                                               m, M->phibar, h->cfg.radius * h->cfg.radius, h->d_lmax);
+  } else {
+    courant_kernel<<<grid, 256, 0, h->stream>>>(h->L, nullptr, nullptr, nullptr, h->S[0].phi, h->S[0].uC,
+                                               h->S[0].vC, m, 0., 0., h->d_lmax);
+  }
+  CCS_TRY(h, cudaGetLastError());
+  unsigned long long bits = 0;
+  CCS_TRY(h, cudaMemcpyAsync(&bits, h->d_lmax, sizeof(bits), cudaMemcpyDeviceToHost, h->stream));
+  CCS_TRY(h, cudaStreamSynchronize(h->stream));
+  double lmax = 0.;
+  std::memcpy(&lmax, &bits, sizeof(lmax));
+  *courant = h->cfg.dt * lmax / std::min(h->cfg.dx, h->cfg.dy);
+  return std::isfinite(*courant) ? CCS_OK : CCS_ERR_NAN;
 }
 
 // ---------------------------------------------------------------------------

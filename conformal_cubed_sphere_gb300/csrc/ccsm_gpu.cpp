@@ -8,7 +8,7 @@
 //            [--scheme RK4|RK3_TVD] [--case 2|5|6|seeded] [--seed K] [--lmax-oro L]
 //            [--dt S | --cfl C] [--radius A] [--run-days D] [--run-hours H] [--run-minutes M]
 //            [--run-seconds S] [--history-interval S] [--energy-of-new-state]
-//            [--autotune] [--out FILE] [--plan]
+//            [--autotune] [--max-courant C] [--out FILE] [--plan]
 //
 // Time settings follow parameters_mod.F90 (defaults :118-128; nsteps = total run
 // time / dt truncated, :149); an output happens after step `it` when
@@ -18,7 +18,9 @@
 // writes phiG, u, v of the final state (FP64, the reference's array layout, one
 // field after the other).  --plan prints the time settings and output steps and
 // exits without touching a GPU.  Every output time runs the health check
-// (ccs_check_state) and stops on a state with non-positive depth or non-finite wind.
+// (ccs_check_state) and stops on a state with non-positive depth or non-finite wind;
+// with --max-courant it also stops when the state's Courant number (ccs_courant)
+// exceeds C.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -35,6 +37,7 @@ struct Options {
   int N = 48, halo = 3, precision = CCS_FP64, scheme = CCS_RK4, ic = CCS_IC_SEEDED, lmax_oro = 0;
   uint64_t seed = 1;
   double dt = 0., cfl = 0.5, radius = 6371229.;  // a of constants_mod.F90:9
+  double max_courant = 0.;                       // 0: no Courant check
   int run_days = 1, run_hours = 0, run_minutes = 0, run_seconds = 0, history_interval = 360;
   bool energy_new = false, autotune = false, plan = false;
   std::string mesh_file, out;
@@ -78,6 +81,7 @@ bool parse(int argc, char **argv, Options &o) {
     else if (a == "--history-interval") o.history_interval = std::atoi(val("--history-interval"));
     else if (a == "--energy-of-new-state") o.energy_new = true;
     else if (a == "--autotune") o.autotune = true;
+    else if (a == "--max-courant") o.max_courant = std::atof(val("--max-courant"));
     else if (a == "--out") o.out = val("--out");
     else if (a == "--plan") o.plan = true;
     else {
@@ -216,6 +220,15 @@ int main(int argc, char **argv) {
       std::fprintf(stderr, "ccsm_gpu: step %d: %lld cells with non-positive depth or non-finite wind\n", it,
                    (long long)nbad);
       return done(1);
+    }
+    if (o.max_courant > 0.) {
+      double courant = 0.;
+      rc = ccs_courant(hd, &courant);
+      if (rc && rc != CCS_ERR_NAN) return done(fail("ccs_courant", rc));
+      if (!(courant <= o.max_courant)) {
+        std::fprintf(stderr, "ccsm_gpu: step %d: Courant number %.4g above %.4g\n", it, courant, o.max_courant);
+        return done(1);
+      }
     }
     // history_write_stat(stat(new)) would write here: ccs_get_state gives stat(new)
     std::printf(" output index/total, MCR, ECR : %zu / %d   %.17g %.17g\n", k + 1, total_output_num,

@@ -67,16 +67,21 @@ class OutputRecord:
     step: int
     mcr: float  # (mass - mass0) / mass0
     ecr: float  # (energy - energy0) / energy0
+    courant: float | None = None  # Courant number of the output state (with max_courant)
 
 
 def run(stepper, ts: TimeSettings, on_output: Callable | None = None, energy_of_new_state: bool = False,
-        log: Callable[[str], None] | None = print, check: bool = True) -> list[OutputRecord]:
+        log: Callable[[str], None] | None = print, check: bool = True,
+        max_courant: float | None = None) -> list[OutputRecord]:
     """Advances `stepper` (a model.Stepper whose state is set) through the run of
     `ts`; calls on_output(output_idx, state) at every history time with the state
     as ccs_get_state returns it (sphere winds included); returns the MCR/ECR records.
     With `check`, every output time also runs the health check (ccs_check_state) and
     a state with non-positive depth or non-finite wind stops the run with
-    FloatingPointError (the reference has no such check and carries on with NaNs)."""
+    FloatingPointError (the reference has no such check and carries on with NaNs).
+    With `max_courant`, every output time also takes the state's Courant number
+    (ccs_courant) into its record and stops the run with FloatingPointError above
+    that bound (the reference's dt is a namelist constant that nothing checks)."""
     if ts.integral_scheme not in ("RK4", "RK3_TVD"):
         raise ValueError(f"integral_scheme {ts.integral_scheme!r}")
     mass0, energy0 = stepper.diag()
@@ -103,9 +108,14 @@ def run(stepper, ts: TimeSettings, on_output: Callable | None = None, energy_of_
             nbad = stepper.check_state()
             if nbad:
                 raise FloatingPointError(f"step {it}: {nbad} cells with non-positive depth or non-finite wind")
+        courant = None
+        if max_courant is not None:
+            courant = stepper.courant()
+            if not courant <= max_courant:
+                raise FloatingPointError(f"step {it}: Courant number {courant:.4g} above {max_courant}")
         if on_output is not None:
             on_output(idx, stepper.get_state())
-        rec = OutputRecord(idx, it, (mass - mass0) / mass0, (energy - energy0) / energy0)
+        rec = OutputRecord(idx, it, (mass - mass0) / mass0, (energy - energy0) / energy0, courant)
         records.append(rec)
         if log:
             log(f" output index/total, MCR, ECR : {idx - 1} / {ts.total_output_num}   {rec.mcr!r} {rec.ecr!r}")

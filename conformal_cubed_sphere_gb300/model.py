@@ -316,6 +316,16 @@ class Stepper:
             L.check(rc, "ccs_check_state", self.handle)
         return n.value
 
+    def courant(self) -> float:
+        """Courant number of the current state (ccs_courant); inf when a cell has
+        non-positive depth or a non-finite value."""
+        c = C.c_double()
+        rc = L.lib().ccs_courant(self.handle, C.byref(c))
+        if rc == L.CCS_ERR_NAN:
+            return float("inf")
+        L.check(rc, "ccs_courant", self.handle)
+        return c.value
+
     def diag(self):
         m, e = C.c_double(), C.c_double()
         L.check(L.lib().ccs_diag(self.handle, C.byref(m), C.byref(e)), "ccs_diag", self.handle)

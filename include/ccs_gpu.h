@@ -200,6 +200,14 @@ int ccs_spatial_operator(ccs_handle *h, double *tend_phiG, double *tend_u, doubl
  * reference has no such check (a blown-up run goes on with NaNs). */
 int ccs_check_state(ccs_handle *h, int64_t *bad_cells);
 
+/* Courant number of the handle's current state: dt * max over interior and
+ * edge-halo cells of max(|uC| + sqrt(IG11 phit), |vC| + sqrt(IG22 phit)) /
+ * min(dx, dy), phit = phi + phis, evaluated on the device in FP64 (the largest
+ * wave speed ccs_cfl_dt takes on the host).  A cell with non-positive phit or a
+ * non-finite value makes it +inf and the call return CCS_ERR_NAN.  No counterpart in
+ * the reference (its time step is a namelist constant). */
+int ccs_courant(ccs_handle *h, double *courant);
+
 /* calc_total_mass / calc_total_energy (diag_mod.F90:10-53) of the current state,
  * as FP64 sums on the device. */
 int ccs_diag(ccs_handle *h, double *total_mass, double *total_energy);

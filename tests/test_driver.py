@@ -178,3 +178,37 @@ def test_run_stops_on_a_bad_state():
     with pytest.raises(FloatingPointError, match="step 6: 3 cells"):
         D.run(Blowup(), ts, log=None)
     assert len(D.run(Blowup(), ts, log=None, check=False)) == 4
+
+
+def test_run_records_and_bounds_the_courant_number():
+    class Growing(_FakeStepper):
+        def courant(self):
+            return 0.1 * self.n
+
+    ts = D.TimeSettings(dt=600.0, run_days=0, run_hours=2, history_interval=1800)
+    recs = D.run(Growing(), ts, log=None, max_courant=5.0)
+    assert [r.courant for r in recs] == pytest.approx([0.3, 0.6, 0.9, 1.2])
+    assert all(r.courant is None for r in D.run(Growing(), ts, log=None))
+    with pytest.raises(FloatingPointError, match="step 9: Courant number 0.9 above 0.8"):
+        D.run(Growing(), ts, log=None, max_courant=0.8)
+
+
+@pytest.mark.gpu
+def test_cpp_driver_stops_above_the_courant_bound():
+    """--max-courant: the C++ driver stops at the first output whose state's Courant
+    number exceeds the bound, and runs through below it."""
+    import subprocess
+
+    from conformal_cubed_sphere_gb300 import _lib as L
+    from conformal_cubed_sphere_gb300 import model as M
+
+    mesh = M.Mesh(12, 3)
+    s = M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=1)
+    dt = float(int(M.cfl_dt(mesh, s, 0.5)))  # whole seconds: the outputs land on the interval
+    args = [_driver_binary(), "--N", "12", "--precision", "mixed", "--case", "seeded", "--radius",
+            str(mesh.radius), "--dt", repr(dt), "--run-days", "0", "--run-seconds", str(int(8 * dt)),
+            "--history-interval", str(int(4 * dt))]
+    ok = subprocess.run(args + ["--max-courant", "5"], capture_output=True, text=True, timeout=600)
+    assert ok.returncode == 0, ok.stderr
+    bad = subprocess.run(args + ["--max-courant", "0.01"], capture_output=True, text=True, timeout=600)
+    assert bad.returncode == 1 and "Courant number" in bad.stderr

@@ -337,3 +337,26 @@ def test_smallest_grids(N, halo):
     x = mx.get_state()
     im = mesh.interior_mask()
     assert max_rel(x["phi"], o["phi"], im) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_courant_number_matches_the_host_cfl(precision):
+    """ccs_courant (device, current state) against the host's CFL step of the same
+    state: dt / cfl_dt(cfl = 1); a state with a negative depth gives inf."""
+    mesh, s, dt = seeded_case(20, 3, seed=9, oro=True)
+    kw = dict(phi_mean=8000.0 * mesh.gravity) if precision == "mixed" else {}
+    g = M.Stepper(mesh, dt, precision=precision, **kw)
+    g.set_state(s)
+    ref = dt / M.cfl_dt(mesh, s, 1.0)
+    assert ref == pytest.approx(0.5, rel=1e-12)  # dt itself came from CFL 0.5
+    tol = 1e-12 if precision == "fp64" else 2e-6  # the mixed lane holds the state in FP32
+    assert g.courant() == pytest.approx(ref, rel=tol)
+    g.step(3)
+    st = g.get_state()
+    assert g.courant() == pytest.approx(dt / M.cfl_dt(mesh, st, 1.0), rel=tol)
+    bad = s.copy()
+    k = np.flatnonzero(mesh.interior_mask())[5]
+    bad["phi"][k] = -(mesh.phis[k] + 1.0)  # phit = phi + phis = -1
+    bad["phiG"][k] = bad["phi"][k] * mesh.sqrtG[k]
+    g.set_state(bad)
+    assert g.courant() == float("inf")
