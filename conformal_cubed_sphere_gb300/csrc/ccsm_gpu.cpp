@@ -9,6 +9,7 @@
 //            [--dt S | --cfl C] [--radius A] [--run-days D] [--run-hours H] [--run-minutes M]
 //            [--run-seconds S] [--history-interval S] [--energy-of-new-state]
 //            [--autotune] [--max-courant C] [--out FILE] [--plan]
+//            [--namelist namelist.input] [--mesh-namelist FILE]
 //
 // Time settings follow parameters_mod.F90 (defaults :118-128; nsteps = total run
 // time / dt truncated, :149); an output happens after step `it` when
@@ -20,12 +21,20 @@
 // exits without touching a GPU.  Every output time runs the health check
 // (ccs_check_state) and stops on a state with non-positive depth or non-finite wind;
 // with --max-courant it also stops when the state's Courant number (ccs_courant)
-// exceeds C.
+// exceeds C.  --namelist reads the dynamic core's namelist.input
+// (parameters_mod.F90:87-113: time_settings, case_select, domain; a mesh_file that
+// exists is read as a raw-binary mesh file) and --mesh-namelist the mesh
+// generator's (N = 90 / dx, mesh_generation/src/parameters_mod.f90:40-50); options
+// after them override what they set.
+#include <cctype>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -49,6 +58,82 @@ const double kGravity = 9.80616, kOmega = 7.292e-5;
 int fail(const char *what, int rc) {
   std::fprintf(stderr, "ccsm_gpu: %s: %s (%d)\n", what, ccs_strerror(rc), rc);
   return 1;
+}
+
+// Fortran namelist file -> {group: {key: value}}, names lower-cased, quotes of
+// string values removed, `!` comments dropped.
+using Namelist = std::map<std::string, std::map<std::string, std::string>>;
+
+std::string lower(std::string t) {
+  for (char &c : t) c = (char)std::tolower((unsigned char)c);
+  return t;
+}
+
+std::string trim(const std::string &t) {
+  size_t a = t.find_first_not_of(" \t\r"), b = t.find_last_not_of(" \t\r");
+  return a == std::string::npos ? std::string() : t.substr(a, b - a + 1);
+}
+
+bool read_namelist(const std::string &path, Namelist &out) {
+  std::ifstream f(path);
+  if (!f) return false;
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string text = ss.str();
+  size_t i = 0;
+  while ((i = text.find('&', i)) != std::string::npos) {
+    size_t e = i + 1;
+    while (e < text.size() && (std::isalnum((unsigned char)text[e]) || text[e] == '_')) e++;
+    const std::string group = lower(text.substr(i + 1, e - i - 1));
+    std::vector<std::string> toks;
+    std::string cur;
+    char q = 0;
+    size_t j = e;
+    for (; j < text.size(); j++) {
+      const char ch = text[j];
+      if (q) {
+        cur += ch;
+        if (ch == q) q = 0;
+      } else if (ch == '\'' || ch == '"') {
+        q = ch;
+        cur += ch;
+      } else if (ch == '!') {
+        while (j < text.size() && text[j] != '\n') j++;
+        toks.push_back(cur);
+        cur.clear();
+      } else if (ch == '/') {
+        break;
+      } else if (ch == ',' || ch == '\n') {
+        toks.push_back(cur);
+        cur.clear();
+      } else {
+        cur += ch;
+      }
+    }
+    toks.push_back(cur);
+    auto &g = out[group];
+    for (const std::string &t : toks) {
+      const size_t eq = t.find('=');
+      if (eq == std::string::npos) continue;
+      std::string v = trim(t.substr(eq + 1));
+      if (v.size() >= 2 && (v[0] == '\'' || v[0] == '"') && v.back() == v[0]) v = v.substr(1, v.size() - 2);
+      g[lower(trim(t.substr(0, eq)))] = v;
+    }
+    i = j + 1;
+  }
+  return true;
+}
+
+// a Fortran real (1.5, 6.0d2, 3E1) as a double
+double fnum(std::string t) {
+  for (char &c : t)
+    if (c == 'd' || c == 'D') c = 'e';
+  return std::atof(t.c_str());
+}
+
+bool file_exists(const std::string &path) {
+  std::ifstream f(path);
+  return (bool)f;
 }
 
 bool parse(int argc, char **argv, Options &o) {
@@ -84,6 +169,56 @@ bool parse(int argc, char **argv, Options &o) {
     else if (a == "--max-courant") o.max_courant = std::atof(val("--max-courant"));
     else if (a == "--out") o.out = val("--out");
     else if (a == "--plan") o.plan = true;
+    else if (a == "--namelist") {
+      const std::string path = val("--namelist");
+      Namelist nml;
+      if (!read_namelist(path, nml)) {
+        std::fprintf(stderr, "ccsm_gpu: cannot read namelist %s\n", path.c_str());
+        return false;
+      }
+      auto &ts = nml["time_settings"];
+      if (ts.count("dt")) o.dt = fnum(ts["dt"]);
+      if (ts.count("run_days")) o.run_days = std::atoi(ts["run_days"].c_str());
+      if (ts.count("run_hours")) o.run_hours = std::atoi(ts["run_hours"].c_str());
+      if (ts.count("run_minutes")) o.run_minutes = std::atoi(ts["run_minutes"].c_str());
+      if (ts.count("run_seconds")) o.run_seconds = std::atoi(ts["run_seconds"].c_str());
+      if (ts.count("history_interval")) o.history_interval = std::atoi(ts["history_interval"].c_str());
+      if (ts.count("integral_scheme")) {
+        const std::string sc = trim(ts["integral_scheme"]);
+        if (sc != "RK4" && sc != "RK3_TVD") {  // parameters_mod.F90:146 stops here
+          std::fprintf(stderr, "ccsm_gpu: unknown integral scheme %s\n", sc.c_str());
+          return false;
+        }
+        o.scheme = sc == "RK3_TVD" ? CCS_RK3_TVD : CCS_RK4;
+      }
+      auto &cs = nml["case_select"];
+      if (cs.count("case_num")) {
+        const int c = std::atoi(cs["case_num"].c_str());
+        o.ic = c == 2 ? CCS_IC_CASE2 : c == 5 ? CCS_IC_CASE5 : c == 6 ? CCS_IC_CASE6 : o.ic;
+      }
+      auto &dom = nml["domain"];
+      if (dom.count("xhalo")) o.halo = std::atoi(dom["xhalo"].c_str());
+      if (dom.count("mesh_file")) {
+        const std::string mf = trim(dom["mesh_file"]);
+        if (file_exists(mf)) o.mesh_file = mf;
+        else std::fprintf(stderr, "ccsm_gpu: mesh_file '%s' not found: the mesh is generated\n", mf.c_str());
+      }
+    } else if (a == "--mesh-namelist") {
+      const std::string path = val("--mesh-namelist");
+      Namelist nml;
+      if (!read_namelist(path, nml)) {
+        std::fprintf(stderr, "ccsm_gpu: cannot read namelist %s\n", path.c_str());
+        return false;
+      }
+      auto &dom = nml["domain"];
+      const double dx = dom.count("dx") ? fnum(dom["dx"]) : 1.;
+      const double n = 90. / dx;
+      if (!(dx > 0.) || std::fabs(n - std::round(n)) > 1e-9) {
+        std::fprintf(stderr, "ccsm_gpu: dx = %g degrees does not divide a panel edge\n", dx);
+        return false;
+      }
+      o.N = (int)std::lround(n);
+    }
     else {
       std::fprintf(stderr, "ccsm_gpu: unknown option %s\n", a.c_str());
       return false;

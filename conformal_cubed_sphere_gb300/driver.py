@@ -50,6 +50,128 @@ class TimeSettings:
         return int(self.nsteps * self.dt / self.history_interval)
 
 
+def _nml_value(tok: str):
+    """One namelist value: a quoted string, a logical, an integer or a real (Fortran
+    d/D exponents accepted)."""
+    t = tok.strip()
+    if len(t) >= 2 and t[0] == t[-1] and t[0] in "'\"":
+        return t[1:-1].replace(t[0] * 2, t[0])
+    low = t.lower()
+    if low in (".true.", ".t.", "t"):
+        return True
+    if low in (".false.", ".f.", "f"):
+        return False
+    try:
+        return int(t)
+    except ValueError:
+        return float(low.replace("d", "e"))
+
+
+def _nml_split(body: str) -> list[str]:
+    """The text of one group split at commas and line ends outside quotes, with `!`
+    comments removed."""
+    out, cur, q = [], [], None
+    i = 0
+    while i < len(body):
+        ch = body[i]
+        if q:
+            cur.append(ch)
+            if ch == q:
+                q = None
+        elif ch in "'\"":
+            q = ch
+            cur.append(ch)
+        elif ch == "!":
+            while i < len(body) and body[i] != "\n":
+                i += 1
+            continue
+        elif ch in ",\n":
+            out.append("".join(cur))
+            cur = []
+        else:
+            cur.append(ch)
+        i += 1
+    out.append("".join(cur))
+    return [t for t in (x.strip() for x in out) if t]
+
+
+def read_namelist(path) -> dict:
+    """The groups of a Fortran namelist file (`&group key = value, ... /`) as
+    {group: {key: value}}, names lower-cased as Fortran compares them; what
+    parameters_mod.F90:readNamelist (:104-113) reads from namelist.input."""
+    text = open(path).read()
+    groups, i = {}, 0
+    while True:
+        a = text.find("&", i)
+        if a < 0:
+            return groups
+        e = a + 1
+        while e < len(text) and (text[e].isalnum() or text[e] == "_"):
+            e += 1
+        name = text[a + 1:e].lower()
+        # the group ends at the first '/' outside quotes and comments
+        j, q, comment = e, None, False
+        while j < len(text):
+            ch = text[j]
+            if comment:
+                comment = ch != "\n"
+            elif q:
+                q = None if ch == q else q
+            elif ch in "'\"":
+                q = ch
+            elif ch == "!":
+                comment = True
+            elif ch == "/":
+                break
+            j += 1
+        entries, key = {}, None
+        for tok in _nml_split(text[e:j]):
+            if "=" in tok and not tok.lstrip().startswith(("'", '"')):
+                k, v = tok.split("=", 1)
+                key = k.strip().lower()
+                entries[key] = _nml_value(v) if v.strip() else None
+            elif key is not None:  # a continued value list
+                prev = entries[key]
+                entries[key] = (prev if isinstance(prev, list) else [prev]) + [_nml_value(tok)]
+        groups[name] = entries
+        i = j + 1
+
+
+@dataclass
+class RunSettings:
+    """What the dynamic core's namelist.input selects (parameters_mod.F90:87-100)."""
+    time: TimeSettings
+    case_num: int = 2
+    mesh_file: str = ""
+    halo: int = 1            # xhalo (parameters_mod.F90:121; the shipped input sets 4)
+    reconstruct_scheme: str = "WENO"
+
+
+def settings_from_namelist(path) -> RunSettings:
+    """RunSettings of a namelist.input, the defaults of parameters_mod.F90:118-128
+    for what it leaves out."""
+    nml = read_namelist(path)
+    ts_g, cs, dom, dyn = (nml.get(g, {}) for g in ("time_settings", "case_select", "domain", "dynamic_opt"))
+    ts = TimeSettings(dt=float(ts_g.get("dt", 300.0)), run_days=int(ts_g.get("run_days", 1)),
+                      run_hours=int(ts_g.get("run_hours", 0)), run_minutes=int(ts_g.get("run_minutes", 0)),
+                      run_seconds=int(ts_g.get("run_seconds", 0)),
+                      history_interval=int(ts_g.get("history_interval", 360)),
+                      integral_scheme=str(ts_g.get("integral_scheme", "RK4")).strip())
+    return RunSettings(ts, int(cs.get("case_num", 2)), str(dom.get("mesh_file", "")).strip(),
+                       int(dom.get("xhalo", 1)), str(dyn.get("reconstruct_scheme", "WENO")).strip())
+
+
+def mesh_resolution_from_namelist(path) -> int:
+    """N of the mesh-generation namelist (mesh_generation/src/parameters_mod.f90:40-50):
+    dx degrees per cell on a 90-degree panel edge."""
+    dom = read_namelist(path).get("domain", {})
+    dx = float(dom.get("dx", 1.0))
+    n = 90.0 / dx
+    if abs(n - round(n)) > 1e-9:
+        raise ValueError(f"dx = {dx} degrees does not divide a panel edge")
+    return int(round(n))
+
+
 def output_steps(ts: TimeSettings) -> list[int]:
     """The steps after which ccsm.F90:55 writes output."""
     hi = float(ts.history_interval)

@@ -212,3 +212,77 @@ def test_cpp_driver_stops_above_the_courant_bound():
     assert ok.returncode == 0, ok.stderr
     bad = subprocess.run(args + ["--max-courant", "0.01"], capture_output=True, text=True, timeout=600)
     assert bad.returncode == 1 and "Courant number" in bad.stderr
+
+
+_NAMELIST = """! settings of one run
+&time_settings
+Run_Days         = 0,
+run_hours        = 6
+run_minutes      = 0
+run_seconds      = 0
+dt               = 6.0d2     ! seconds
+history_interval = 3600
+integral_scheme  = 'RK3_TVD' ! 'RK3_TVD' or 'RK4', a '/' in a comment
+/
+
+&case_select
+case_num    = 6,
+/
+
+&domain
+mesh_file   = 'no/such/mesh!file'
+xhalo       = 4,  yhalo = 4,
+/
+
+&dynamic_opt
+reconstruct_scheme = "WENO"
+/
+"""
+
+
+def test_namelist_reader(tmp_path):
+    path = tmp_path / "namelist.input"
+    path.write_text(_NAMELIST)
+    nml = D.read_namelist(path)
+    assert nml["time_settings"]["run_days"] == 0 and nml["time_settings"]["dt"] == 600.0
+    assert nml["time_settings"]["integral_scheme"] == "RK3_TVD"
+    assert nml["domain"] == {"mesh_file": "no/such/mesh!file", "xhalo": 4, "yhalo": 4}
+    rs = D.settings_from_namelist(path)
+    assert rs.time == D.TimeSettings(dt=600.0, run_days=0, run_hours=6, history_interval=3600,
+                                     integral_scheme="RK3_TVD")
+    assert (rs.case_num, rs.mesh_file, rs.halo, rs.reconstruct_scheme) == (6, "no/such/mesh!file", 4, "WENO")
+    # an empty file gives the defaults of parameters_mod.F90:118-128
+    empty = tmp_path / "empty.input"
+    empty.write_text("")
+    assert D.settings_from_namelist(empty).time == D.TimeSettings()
+    # value lists and logicals
+    other = tmp_path / "other.input"
+    other.write_text("&g\n a = 1, 2, 3\n flag = .true.\n s = 'it''s'\n/\n")
+    assert D.read_namelist(other)["g"] == {"a": [1, 2, 3], "flag": True, "s": "it's"}
+
+
+def test_mesh_namelist_resolution(tmp_path):
+    path = tmp_path / "mesh.input"
+    path.write_text("&domain\n dx = 0.5,\n dy = 0.5,\n gen_method = 'Rancic'\n/\n")
+    assert D.mesh_resolution_from_namelist(path) == 180
+    path.write_text("&domain\n dx = 0.7\n/\n")
+    with pytest.raises(ValueError):
+        D.mesh_resolution_from_namelist(path)
+
+
+def test_cpp_driver_reads_the_namelists(tmp_path):
+    """ccsm_gpu --namelist / --mesh-namelist (host only, --plan): the same time
+    settings, scheme, halo and resolution as the Python reader."""
+    import subprocess
+
+    nl = tmp_path / "namelist.input"
+    nl.write_text(_NAMELIST)
+    ml = tmp_path / "mesh.input"
+    ml.write_text("&domain\n dx = 7.5,\n dy = 7.5\n/\n")
+    r = subprocess.run([_driver_binary(), "--namelist", str(nl), "--mesh-namelist", str(ml), "--plan"],
+                       capture_output=True, text=True, check=True)
+    rs = D.settings_from_namelist(nl)
+    steps = [int(l.split()[-1]) for l in r.stdout.splitlines() if l.startswith(" output step")]
+    assert steps == D.output_steps(rs.time)
+    assert f" N 12 halo 4 dt 600 nsteps {rs.time.nsteps} " in r.stdout
+    assert "mesh_file 'no/such/mesh!file' not found" in r.stderr
