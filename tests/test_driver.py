@@ -286,3 +286,30 @@ def test_cpp_driver_reads_the_namelists(tmp_path):
     assert steps == D.output_steps(rs.time)
     assert f" N 12 halo 4 dt 600 nsteps {rs.time.nsteps} " in r.stdout
     assert "mesh_file 'no/such/mesh!file' not found" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cpp_driver_runs_a_namelist_case_like_the_python_driver(tmp_path):
+    """A run set up only by namelist files (test case 6, RK3_TVD, halo 4, C12 from
+    dx = 7.5): the C++ driver's MCR/ECR lines equal the Python driver's records on
+    the same case bit for bit (FP64 lane)."""
+    import subprocess
+
+    from conformal_cubed_sphere_gb300 import _lib as L
+    from conformal_cubed_sphere_gb300 import model as M
+
+    nl = tmp_path / "namelist.input"
+    nl.write_text(_NAMELIST)
+    ml = tmp_path / "mesh.input"
+    ml.write_text("&domain\n dx = 7.5,\n dy = 7.5\n/\n")
+    r = subprocess.run([_driver_binary(), "--namelist", str(nl), "--mesh-namelist", str(ml), "--precision", "fp64"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    got = [tuple(float(x) for x in l.split()[-2:]) for l in r.stdout.splitlines() if "MCR, ECR" in l][1:]
+    rs = D.settings_from_namelist(nl)
+    mesh = M.Mesh(D.mesh_resolution_from_namelist(ml), rs.halo, radius=6371229.0)
+    s = M.initial_state(mesh, kind={2: L.CCS_IC_CASE2, 5: L.CCS_IC_CASE5, 6: L.CCS_IC_CASE6}[rs.case_num])
+    g = M.Stepper(mesh, rs.time.dt, precision="fp64", scheme=rs.time.integral_scheme)
+    g.set_state(s)
+    recs = D.run(g, rs.time, log=None)
+    assert got == [(rec.mcr, rec.ecr) for rec in recs]
