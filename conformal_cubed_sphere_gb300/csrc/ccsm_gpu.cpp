@@ -8,7 +8,7 @@
 //            [--scheme RK4|RK3_TVD] [--case 2|5|6|seeded] [--seed K] [--lmax-oro L]
 //            [--dt S | --cfl C] [--radius A] [--run-days D] [--run-hours H] [--run-minutes M]
 //            [--run-seconds S] [--history-interval S] [--energy-of-new-state]
-//            [--autotune] [--max-courant C] [--out FILE] [--plan]
+//            [--autotune] [--max-courant C] [--out FILE] [--history PREFIX] [--plan]
 //            [--namelist namelist.input] [--mesh-namelist FILE]
 //
 // Time settings follow parameters_mod.F90 (defaults :118-128; nsteps = total run
@@ -25,7 +25,10 @@
 // (parameters_mod.F90:87-113: time_settings, case_select, domain; a mesh_file that
 // exists is read as a raw-binary mesh file) and --mesh-namelist the mesh
 // generator's (N = 90 / dx, mesh_generation/src/parameters_mod.f90:40-50); options
-// after them override what they set.
+// after them override what they set.  --history PREFIX writes the state of every
+// history time, the initial one included, as checkpoint files PREFIX_NNNN.ccsstate
+// (ccs_state_write; the place of history_write_stat, ccsm.F90:44,60, whose NetCDF
+// output needs a library this program does not link).
 #include <cctype>
 #include <cmath>
 #include <cstdint>
@@ -49,7 +52,7 @@ struct Options {
   double max_courant = 0.;                       // 0: no Courant check
   int run_days = 1, run_hours = 0, run_minutes = 0, run_seconds = 0, history_interval = 360;
   bool energy_new = false, autotune = false, plan = false;
-  std::string mesh_file, out;
+  std::string mesh_file, out, history;
 };
 
 // constants_mod.F90:6-12
@@ -168,6 +171,7 @@ bool parse(int argc, char **argv, Options &o) {
     else if (a == "--autotune") o.autotune = true;
     else if (a == "--max-courant") o.max_courant = std::atof(val("--max-courant"));
     else if (a == "--out") o.out = val("--out");
+    else if (a == "--history") o.history = val("--history");
     else if (a == "--plan") o.plan = true;
     else if (a == "--namelist") {
       const std::string path = val("--namelist");
@@ -335,6 +339,17 @@ int main(int argc, char **argv) {
   }
   double mass0 = 0., energy0 = 0.;
   if ((rc = ccs_diag(hd, &mass0, &energy0))) return done(fail("ccs_diag", rc));
+  // history output (ccsm.F90:44,60): the state as ccs_get_state gives it
+  auto write_history = [&](int idx) -> int {
+    if (o.history.empty()) return 0;
+    int r = ccs_get_state(hd, &sv);
+    if (r) return fail("ccs_get_state", r);
+    char name[32];
+    std::snprintf(name, sizeof(name), "_%04d.ccsstate", idx);
+    if ((r = ccs_state_write((o.history + name).c_str(), N, h, &sv))) return fail("ccs_state_write", r);
+    return 0;
+  };
+  if (write_history(1)) return done(1);
   std::printf(" output index/total, MCR, ECR : %d / %d   %.17g %.17g\n", 0, total_output_num, 0., 0.);
   int stepped = 0;
   for (size_t k = 0; k < outputs.size(); k++) {
@@ -365,7 +380,7 @@ int main(int argc, char **argv) {
         return done(1);
       }
     }
-    // history_write_stat(stat(new)) would write here: ccs_get_state gives stat(new)
+    if (write_history((int)k + 2)) return done(1);  // history_write_stat(stat(new), output_idx)
     std::printf(" output index/total, MCR, ECR : %zu / %d   %.17g %.17g\n", k + 1, total_output_num,
                 (mass - mass0) / mass0, (energy - energy0) / energy0);
   }

@@ -313,3 +313,38 @@ def test_cpp_driver_runs_a_namelist_case_like_the_python_driver(tmp_path):
     g.set_state(s)
     recs = D.run(g, rs.time, log=None)
     assert got == [(rec.mcr, rec.ecr) for rec in recs]
+
+
+@pytest.mark.gpu
+def test_cpp_driver_history_files(tmp_path):
+    """--history: one checkpoint file per history time (the initial state included),
+    each equal to the Python driver's output state at that time."""
+    import subprocess
+
+    import numpy as np
+
+    from conformal_cubed_sphere_gb300 import _lib as L
+    from conformal_cubed_sphere_gb300 import model as M
+
+    nl = tmp_path / "namelist.input"
+    nl.write_text(_NAMELIST)
+    ml = tmp_path / "mesh.input"
+    ml.write_text("&domain\n dx = 7.5\n/\n")
+    prefix = tmp_path / "hist"
+    r = subprocess.run([_driver_binary(), "--namelist", str(nl), "--mesh-namelist", str(ml), "--precision", "fp64",
+                        "--history", str(prefix)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rs = D.settings_from_namelist(nl)
+    mesh = M.Mesh(12, rs.halo, radius=6371229.0)
+    s = M.initial_state(mesh, kind=L.CCS_IC_CASE6)
+    g = M.Stepper(mesh, rs.time.dt, precision="fp64", scheme=rs.time.integral_scheme)
+    g.set_state(s)
+    states = {}
+    D.run(g, rs.time, on_output=lambda idx, st: states.__setitem__(idx, st), log=None)
+    files = sorted(tmp_path.glob("hist_*.ccsstate"))
+    assert [f.name for f in files] == [f"hist_{k:04d}.ccsstate" for k in sorted(states)]
+    m = ~mesh.corner_mask()
+    for f, k in zip(files, sorted(states)):
+        got = M.State.load(f, mesh)
+        for name in ("phiG", "u", "v", "phi"):
+            assert np.array_equal(got[name][m], states[k][name][m]), (f.name, name)
