@@ -145,3 +145,27 @@ def test_generated_meshes_pass_the_panel_symmetry_check():
         assert rc != L.CCS_ERR_UNSUPPORTED and rc != L.CCS_ERR_ARG, rc
         if rc == 0:
             L.lib().ccs_destroy(hd)
+
+
+def test_cfl_dt_is_the_largest_wave_speed_restated():
+    """ccs_cfl_dt against a numpy restatement: cfl * min(dx, dy) over the largest
+    max(|uC| + sqrt(IG11 phit), |vC| + sqrt(IG22 phit)) of the interior and edge-halo
+    cells; a non-positive depth makes it undefined (-1)."""
+    mesh = M.Mesh(10, 3)
+    s = M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=4, lmax_oro=6)
+    h, N = mesh.halo, mesh.N
+    idx = np.arange(mesh.nh) - h + 1
+    inb = (idx >= 0) & (idx <= N + 1)
+    out_i = (idx < 1) | (idx > N)
+    sel = (inb[:, None] & inb[None, :]) & ~(out_i[:, None] & out_i[None, :])
+    sel = np.repeat(sel[:, :, None], 6, axis=2).reshape(-1, order="F")
+    pt = s["phi"] + mesh.phis
+    ig = mesh.matrixIG.reshape(-1, 4)
+    lx = np.abs(s["uC"]) + np.sqrt(ig[:, 0] * pt)
+    ly = np.abs(s["vC"]) + np.sqrt(ig[:, 3] * pt)
+    lmax = np.max(np.maximum(lx, ly)[sel])
+    assert M.cfl_dt(mesh, s, 0.5) == pytest.approx(0.5 * min(mesh.dx, mesh.dy) / lmax, rel=1e-15)
+    bad = s.copy()
+    bad["phi"][np.flatnonzero(mesh.interior_mask())[0]] = -1e6
+    with pytest.raises(ValueError):
+        M.cfl_dt(mesh, bad, 0.5)
