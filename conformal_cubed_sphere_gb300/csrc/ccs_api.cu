@@ -153,6 +153,7 @@ struct ccs_handle {
   // timing
   bool timing = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_order = nullptr;  // orders the handle's stream with a batch step
   double kernel_ms = 0.;
   int64_t launches = 0;
   // diagnostics
@@ -578,6 +579,7 @@ void ccs_destroy(ccs_handle *h) {
   if (h->d_lmax) cudaFree(h->d_lmax);
   if (h->mixed) mixed_handle_destroy(h);
   if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev_order) cudaEventDestroy(h->ev_order);
   if (h->ev1) cudaEventDestroy(h->ev1);
   h->mesh.reset();
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1361,6 +1363,7 @@ struct ccs_batch {
   std::vector<ccs_handle *> members;
   cudaStream_t stream = nullptr;
   cudaEvent_t fork = nullptr;
+  cudaEvent_t after = nullptr;  // end of the last enqueued step, for the members' streams
   int device = 0;
   cudaGraphExec_t g_step = nullptr, g_step_sw = nullptr;
   std::string err;
@@ -1448,6 +1451,7 @@ extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **o
   b->members.assign(members, members + n);
   cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming);
   auto member_var = [](const ccs_handle *m) { return m->cfg.precision == CCS_MIXED ? m->mixed->var : m->var; };
   for (int lane = 0; lane < 2; lane++)
     for (int scheme = 0; scheme < 2; scheme++)
@@ -1530,9 +1534,20 @@ static int batch_step(ccs_batch *b, int nsteps, bool sync) {
     if (!rc) rc = batch_capture(b, true, &b->g_step_sw);
     if (rc) return rc;
   }
+  // the step starts after the members' own pending work (an asynchronous upload and
+  // its import, an asynchronous step) and the members' later work after the step
+  for (ccs_handle *h : b->members) {
+    if (!h->ev_order && cudaEventCreateWithFlags(&h->ev_order, cudaEventDisableTiming) != cudaSuccess)
+      return CCS_ERR_CUDA;
+    if (cudaEventRecord(h->ev_order, h->stream) != cudaSuccess) return CCS_ERR_CUDA;
+    if (cudaStreamWaitEvent(b->stream, h->ev_order, 0) != cudaSuccess) return CCS_ERR_CUDA;
+  }
   for (int s = 0; s < nsteps - 1; s++)
     if (cudaGraphLaunch(b->g_step, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
   if (cudaGraphLaunch(b->g_step_sw, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  if (cudaEventRecord(b->after, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  for (ccs_handle *h : b->members)
+    if (cudaStreamWaitEvent(h->stream, b->after, 0) != cudaSuccess) return CCS_ERR_CUDA;
   if (sync && cudaStreamSynchronize(b->stream) != cudaSuccess) return CCS_ERR_CUDA;
   for (ccs_handle *h : b->members) h->sphere_valid = true;
   return CCS_OK;
@@ -1555,6 +1570,7 @@ extern "C" void ccs_batch_destroy(ccs_batch *b) {
     if (g.stream) cudaStreamDestroy(g.stream);
   }
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->after) cudaEventDestroy(b->after);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }

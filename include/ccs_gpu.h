@@ -232,7 +232,11 @@ int ccs_diag_noalloc(int N, int halo, const double *phiG, const double *phi, con
 /* ---- ensembles and uneven batches ---------------------------------------- */
 
 /* Groups handles (any mix of N, dt and lanes) so that each RK stage of all members
- * runs as one launch per lane over a shared work list, captured in a CUDA graph. */
+ * runs as one launch per lane over a shared work list, captured in a CUDA graph.
+ * A batch step is ordered after each member's pending work on its own stream (an
+ * asynchronous upload and its import, an asynchronous step), and each member's later
+ * work after the batch step, so the members' *_async calls and ccs_batch_step_async
+ * compose in call order. */
 int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out);
 int ccs_batch_step(ccs_batch *b, int nsteps);
 /* Same, enqueued on the batch's stream (ccs_batch_stream) without waiting. */

@@ -229,3 +229,36 @@ def test_long_run_stays_healthy_and_conserves_mass():
     assert g.check_state() == 0
     m1, _ = g.diag()
     assert abs(m1 - m0) / abs(m0) < 1e-9
+
+
+def test_member_async_transfers_around_an_async_batch_step():
+    """Members' asynchronous uploads, an asynchronous batch step and the members'
+    asynchronous downloads, in call order with no synchronisation between them: the
+    batch waits for the uploads and the downloads wait for the batch (bit for bit
+    the single runs)."""
+    mesh = M.Mesh(48, 3)
+    first = [M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=80 + k) for k in range(3)]
+    inputs = [M.initial_state(mesh, kind=L.CCS_IC_SEEDED, seed=90 + k, h_rms=220.0) for k in range(3)]
+    dt = min(M.cfl_dt(mesh, st, 0.5) for st in first + inputs)
+    kw = dict(phi_mean=8000.0 * mesh.gravity)
+    lanes = ("mixed", "mixed", "fp64")
+    members = [M.Stepper(mesh, dt, precision=lane, **(kw if lane == "mixed" else {})) for lane in lanes]
+    for m, st in zip(members, first):
+        m.set_state(st)
+    batch = M.Batch(members)
+    for m, st in zip(members, inputs):
+        m.set_state_async(st)
+    batch.step_async(2)
+    outs = [M.State.zeros(mesh) for _ in members]
+    for m, o in zip(members, outs):
+        m.get_state_async(o)
+    for m in members:
+        m.sync()
+    msk = valid_mask(mesh)
+    for lane, st, o in zip(lanes, inputs, outs):
+        r = M.Stepper(mesh, dt, precision=lane, **(kw if lane == "mixed" else {}))
+        r.set_state(st)
+        r.step(2)
+        ref = r.get_state()
+        for k in CHECK_FIELDS:
+            assert bitwise_equal(o[k], ref[k], msk), (lane, k)
