@@ -236,7 +236,9 @@ int ccs_diag_noalloc(int N, int halo, const double *phiG, const double *phi, con
  * A batch step is ordered after each member's pending work on its own stream (an
  * asynchronous upload and its import, an asynchronous step), and each member's later
  * work after the batch step, so the members' *_async calls and ccs_batch_step_async
- * compose in call order. */
+ * compose in call order.  The batch keeps each member's tile variant and operator
+ * as they were at creation, and the members must outlive it (ccs_batch_destroy
+ * first). */
 int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out);
 int ccs_batch_step(ccs_batch *b, int nsteps);
 /* Same, enqueued on the batch's stream (ccs_batch_stream) without waiting. */
