@@ -244,3 +244,66 @@ def run(stepper, ts: TimeSettings, on_output: Callable | None = None, energy_of_
     if ts.nsteps > done:
         stepper.step(ts.nsteps - done)
     return records
+
+
+def history_writer(prefix: str, mesh) -> Callable:
+    """An on_output callback writing each history state as the checkpoint file
+    `prefix_NNNN.ccsstate` (the files `ccsm_gpu --history` writes)."""
+    def write(idx, state):
+        state.save(f"{prefix}_{idx:04d}.ccsstate", mesh)
+    return write
+
+
+def main(argv=None) -> int:
+    """The model program (ccsm.F90) from the reference's namelist files, on the GPU:
+    python -m conformal_cubed_sphere_gb300.driver --namelist namelist.input
+    [--mesh-namelist FILE | --N N] [--precision fp64|mixed] [--history PREFIX]
+    [--max-courant C] [--radius A].  The mesh is generated (conformal cubic map) or
+    read from the namelist's mesh_file when that is a raw-binary mesh file."""
+    import argparse
+    import os
+
+    from . import _lib as L
+    from . import model as M
+
+    ap = argparse.ArgumentParser(description="ccsm.F90 time loop on the GPU step")
+    ap.add_argument("--namelist", required=True)
+    ap.add_argument("--mesh-namelist", default=None)
+    ap.add_argument("--N", type=int, default=None)
+    ap.add_argument("--precision", choices=("fp64", "mixed"), default="fp64")
+    ap.add_argument("--radius", type=float, default=6371229.0)  # constants_mod.F90:9
+    ap.add_argument("--history", default=None)
+    ap.add_argument("--max-courant", type=float, default=None)
+    ap.add_argument("--energy-of-new-state", action="store_true")
+    a = ap.parse_args(argv)
+    rs = settings_from_namelist(a.namelist)
+    if rs.time.integral_scheme not in ("RK4", "RK3_TVD"):
+        print(f"unknown integral scheme {rs.time.integral_scheme}")  # parameters_mod.F90:146
+        return 2
+    if rs.mesh_file and os.path.exists(rs.mesh_file):
+        mesh = M.Mesh.from_file(rs.mesh_file, halo=rs.halo, radius=a.radius)
+    else:
+        N = a.N or (mesh_resolution_from_namelist(a.mesh_namelist) if a.mesh_namelist else None)
+        if N is None:
+            ap.error("no mesh: give --N or --mesh-namelist (or a raw-binary mesh_file in the namelist)")
+        mesh = M.Mesh(N, rs.halo, radius=a.radius)
+    kind = {2: L.CCS_IC_CASE2, 5: L.CCS_IC_CASE5, 6: L.CCS_IC_CASE6}.get(rs.case_num)
+    if kind is None:
+        print(f"unknown case_num {rs.case_num}")
+        return 2
+    state = M.initial_state(mesh, kind=kind)
+    stepper = M.Stepper(mesh, rs.time.dt, precision=a.precision, scheme=rs.time.integral_scheme)
+    stepper.set_state(state)
+    print(f" Temporal integration scheme is {rs.time.integral_scheme}")
+    on_output = history_writer(a.history, mesh) if a.history else None
+    try:
+        run(stepper, rs.time, on_output=on_output, energy_of_new_state=a.energy_of_new_state,
+            max_courant=a.max_courant)
+    except FloatingPointError as e:
+        print(f"stopped: {e}")
+        return 1
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -348,3 +348,41 @@ def test_cpp_driver_history_files(tmp_path):
         got = M.State.load(f, mesh)
         for name in ("phiG", "u", "v", "phi"):
             assert np.array_equal(got[name][m], states[k][name][m]), (f.name, name)
+
+
+@pytest.mark.gpu
+def test_python_driver_cli_matches_the_cpp_driver(tmp_path):
+    """python -m conformal_cubed_sphere_gb300.driver and ccsm_gpu on the same
+    namelist files: the same MCR/ECR values and byte-identical history files."""
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    nl = tmp_path / "namelist.input"
+    nl.write_text(_NAMELIST)
+    ml = tmp_path / "mesh.input"
+    ml.write_text("&domain\n dx = 7.5\n/\n")
+    common = ["--namelist", str(nl), "--mesh-namelist", str(ml), "--precision", "fp64"]
+    c = subprocess.run([_driver_binary()] + common + ["--history", str(tmp_path / "c")], capture_output=True,
+                       text=True, timeout=600)
+    p = subprocess.run([sys.executable, "-m", "conformal_cubed_sphere_gb300.driver"] + common +
+                       ["--history", str(tmp_path / "p")], capture_output=True, text=True, timeout=600,
+                       cwd=Path(__file__).resolve().parents[1])
+    assert c.returncode == 0, c.stderr
+    assert p.returncode == 0, p.stderr + p.stdout
+
+    def values(out):
+        return [tuple(float(x) for x in l.split()[-2:]) for l in out.splitlines() if "MCR, ECR" in l]
+
+    assert values(c.stdout) == values(p.stdout) and len(values(p.stdout)) == 7
+    cf, pf = sorted(tmp_path.glob("c_*.ccsstate")), sorted(tmp_path.glob("p_*.ccsstate"))
+    assert len(cf) == len(pf) == 7
+    for a, b in zip(cf, pf):
+        assert a.read_bytes() == b.read_bytes(), (a.name, b.name)
+
+
+def test_python_driver_cli_needs_a_mesh(tmp_path):
+    nl = tmp_path / "namelist.input"
+    nl.write_text(_NAMELIST)
+    with pytest.raises(SystemExit):
+        D.main(["--namelist", str(nl)])
