@@ -964,10 +964,10 @@ static int mixed_build_stages(ccs_handle *h) {
 static void mixed_handle_destroy(ccs_handle *h) {
   MixedLane *M = h->mixed;
   if (!M) return;
-  if (M->g_step) cudaGraphExecDestroy(M->g_step);
-  if (M->buf) cudaFree(M->buf);
   if (M->cin) cudaStreamSynchronize(M->cin);
   if (M->cout) cudaStreamSynchronize(M->cout);
+  if (M->g_step) cudaGraphExecDestroy(M->g_step);
+  if (M->buf) cudaFree(M->buf);
   for (int k = 0; k < 2; k++)
     for (cudaEvent_t e : {M->in_ready[k], M->in_free[k], M->out_ready[k], M->out_free[k]})
       if (e) cudaEventDestroy(e);
