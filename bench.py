@@ -7,26 +7,32 @@ halo 3) from the seeded state with orography (spherical harmonics, h = 8000 m +
 FP32/FP64 lane; the FP64 parity lane is measured beside it on the same state.
 
   value      device-timed throughput, inputs resident in HBM, L2 flushed between
-             timed steps (CUDA events on the library's own stream)
+             timed steps (CUDA events on the library's own stream around each
+             step: one graph of four stage launches)
   e2e        the same metric through the C ABI with host buffers: every step is
              ccs_set_state_async of its input (pinned host -> device) +
              ccs_step_async(1) + ccs_get_state_async of its result (device ->
              pinned host), one ccs_sync at the end, so one step's copies overlap
-             the neighbouring steps; the synchronous calls are reported beside it
-  roofline   the mixed stage kernel's average launch duration against the
-             measured HBM copy bandwidth; roofline.issue puts the same launches
-             against the bound the kernel actually has, instruction issue
+             the neighbouring steps; the synchronous calls are reported beside it,
+             and the host link's own rates for the same bytes (link_*_gbs)
+  roofline   the mixed stage kernel (a quarter of the timed step) against the
+             measured HBM copy bandwidth; roofline.issue puts it against the bound
+             the kernel actually has, instruction issue
+  ensemble   64 x C96 members in one launch per RK stage (graph-captured) against
+             the same members stepped one after another
+  uneven     16 x C48 + 8 x C96 + 4 x C192 + 1 x C384, FP64 and mixed members in one
+             batch (one launch per lane and RK stage)
   cpu_baseline  the CPU FP64 oracle (a restatement of the reference step) on the
              host cores, on a bounded sample of the workload
 
 --impl reference times only the reference CPU step (the oracle) on the same
-workload and prints its own line.  Under torchrun (N > 1) every rank advances
-its own C384 replica (the single-member step does not shard): value is the
-total over ranks divided by the slowest rank's time.  --workload ensemble (64 x
-C96 members per GPU, sharded by member across ranks) and --workload uneven
-(16 x C48 + 8 x C96 + 4 x C192 + 1 x C384, FP64 and mixed members together)
-print their own lines.  Tile shapes come from the autotuner (--tile-variant
-pins the mixed one for profiling runs).
+workload and prints its own line; its inputs come from oracle/case_setup.py, so that
+process maps no file of the CUDA library.  Under torchrun (N > 1) every rank
+advances its own C384 replica (the single-member step does not shard): value is
+the total over ranks divided by the slowest rank's time; the ensemble shards by
+member.  --workload ensemble and --workload uneven print only those lines.  Tile
+shapes come from the autotuner (--tile-variant pins the mixed one for profiling
+runs).
 """
 from __future__ import annotations
 
@@ -55,8 +61,10 @@ ALG_BYTES_FP64 = 600.0
 
 
 def _dist():
-    from conformal_cubed_sphere_gb300.parallel import dist_env
-    return dist_env()
+    """(world_size, rank, local_rank) from the torchrun environment (read here, so
+    that the reference arm imports nothing of the package)."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 class ClockSampler:
@@ -115,16 +123,31 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_per_launch(name: str):
-    """dram bytes per launch from the committed ncu summary, if present."""
+# the sources of the stage kernels whose ncu counters profiles/roofline_traffic.json holds
+KERNEL_SOURCES = ("ccs_mixed.cu", "ccs_fp64.cu", "ccs_kernels.h", "ccs_internal.h")
+
+
+def kernel_sources_hash() -> str:
+    """First 16 hex digits of the SHA-256 of the stage kernels' sources."""
+    import hashlib
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        h.update((ROOT / "conformal_cubed_sphere_gb300" / "csrc" / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def profiled_counters() -> dict:
+    """The ncu counters of profiles/roofline_traffic.json, only when they were taken on
+    this build of the stage kernels (its sources_sha16 equals kernel_sources_hash());
+    {} otherwise, so that a kernel edit never leaves stale counters on the line."""
     p = ROOT / "profiles" / "roofline_traffic.json"
     if not p.exists():
-        return None
+        return {}
     try:
         d = json.loads(p.read_text())
-        return d.get(name)
     except Exception:
-        return None
+        return {}
+    return d if d.get("sources_sha16") == kernel_sources_hash() else {}
 
 
 def fp64_roofline(avg_ms, fp64_inst, sms, clocks):
@@ -179,13 +202,6 @@ def time_device_steps(stepper, torch, steps: int, flush: "torch.Tensor"):
         ev1.synchronize()
         total += ev0.elapsed_time(ev1)
     return total / 1e3  # seconds
-
-
-def kernel_launch_avg_ms(stepper, steps: int):
-    stepper.timing(enable=1, reset=1)
-    stepper.step(steps)
-    ms, n = stepper.timing(enable=0, reset=1)
-    return ms / max(n, 1), n
 
 
 def pinned_state(M, mesh, torch, order, fill=None):
@@ -249,6 +265,43 @@ def e2e_rate(stepper, mesh, state, steps: int, torch):
     return el_async, el_sep, el_sync, n_in * nb, n_out * nb
 
 
+def link_rates(torch, dev: int, h2d_bytes: int, d2h_bytes: int, reps: int = 5) -> dict:
+    """The host link alone, for one step's bytes: one pinned upload of h2d_bytes, one
+    pinned download of d2h_bytes, and both at once on two streams; CUDA events, best
+    of `reps` after a warm-up round.  The e2e loop cannot beat `both_ms` per step."""
+    hin = torch.empty(h2d_bytes, dtype=torch.uint8).pin_memory()
+    hout = torch.empty(d2h_bytes, dtype=torch.uint8).pin_memory()
+    din = torch.empty(h2d_bytes, dtype=torch.uint8, device=dev)
+    dout = torch.empty(d2h_bytes, dtype=torch.uint8, device=dev)
+    s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def timed(up: bool, down: bool) -> float:
+        best = None
+        for r in range(reps + 1):
+            torch.cuda.synchronize(dev)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(s_up)
+            s_down.wait_event(e0)
+            if up:
+                with torch.cuda.stream(s_up):
+                    din.copy_(hin, non_blocking=True)
+            if down:
+                with torch.cuda.stream(s_down):
+                    hout.copy_(dout, non_blocking=True)
+            e1.record(s_up)
+            e2.record(s_down)
+            torch.cuda.synchronize(dev)
+            ms = max(e0.elapsed_time(e1), e0.elapsed_time(e2))
+            if r > 0 and (best is None or ms < best):
+                best = ms
+        return best
+
+    t_up, t_down, t_both = timed(True, False), timed(False, True), timed(True, True)
+    return {"link_h2d_gbs": h2d_bytes / t_up / 1e6, "link_d2h_gbs": d2h_bytes / t_down / 1e6,
+            "link_both_ms": t_both, "how": "one pinned copy per direction of the e2e step's bytes, CUDA events, "
+                                           "best of %d; both = the two copies at once on two streams" % reps}
+
+
 def cpu_baseline(mesh, state, dt, seconds=10.0):
     """The oracle on all host cores, on a sample of about `seconds` of CPU work:
     as many C384 RK4 steps as one warm-up step says fit (at most 300)."""
@@ -270,14 +323,18 @@ def cpu_baseline(mesh, state, dt, seconds=10.0):
 
 
 def run_reference(args):
+    """The reference CPU step (the oracle) on all host cores.  Its inputs come from
+    oracle/case_setup.py (the host set-up code built for the CPU alone), so this
+    process maps no file of the CUDA library; they equal the GPU arm's bit for bit."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    mesh, s, dt = build_case()
+    from oracle import case_setup as CS
     from oracle import oracle as O
+    mesh, s, dt = CS.seeded_case(N_BENCH, HALO, seed=SEED, lmax_oro=8)
     threads = os.cpu_count() or 1
     orc = O.Oracle.from_mesh(mesh, threads=threads)
-    orc.set_state(s.arrays)
+    orc.set_state(s)
     # one step = one RK4 step of C384 on all host cores (about 0.1 s on 16 Grace
     # cores); K and W are honoured up to 600 and 5
     steps = max(1, min(args.steps, 600))
@@ -292,7 +349,8 @@ def run_reference(args):
         "impl": "reference", "metric": "C384 cell-steps/s", "value": v, "unit": "cell-steps/s",
         "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "C384 seeded state with orography, RK4, CFL 0.5", "N": mesh.N, "halo": HALO},
+        "config": {"workload": "C384 seeded state with orography, RK4, CFL 0.5", "N": mesh.N, "halo": HALO,
+                   "inputs": "oracle/case_setup.py (CPU-only set-up library; no CUDA library mapped)"},
         "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": O.lib().orc_get_threads(), "kind": "port",
                          "sample": f"{steps} RK4 steps of C384 after {warm} warm-up step(s)"},
         "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -311,17 +369,17 @@ def _batch_time(batch, torch, steps: int):
     return ev0.elapsed_time(ev1) / 1e3
 
 
-def run_ensemble(args, torch):
-    """`members` members at C96 per GPU (seed + k, RMS 150-250 m, wind 30-50 m/s),
-    mixed lane, one launch per RK stage for all of a rank's members, graph-captured;
-    against the same members advanced one after another through their own handles.
-    Under torchrun the ensemble is members x ranks, sharded round robin by member
-    with no collective on the data path (weak scaling)."""
+def run_ensemble(torch, members_per_gpu: int, steps: int, warmup: int) -> dict:
+    """`members_per_gpu` members at C96 per GPU (seed + k, RMS 150-250 m, wind 30-50
+    m/s), mixed lane, one launch per RK stage for all of a rank's members,
+    graph-captured; against the same members advanced one after another through
+    their own handles.  Under torchrun the ensemble is members x ranks, sharded round
+    robin by member with no collective on the data path (weak scaling)."""
     from conformal_cubed_sphere_gb300 import model as M
     from conformal_cubed_sphere_gb300.parallel import shard_members, slowest_rank_seconds
     ws, rank, _ = _dist()
     N = 96
-    total = args.members * ws
+    total = members_per_gpu * ws
     mine = shard_members(total, rank, ws)
     n = len(mine)
     mesh = M.Mesh(N, HALO)
@@ -335,11 +393,12 @@ def run_ensemble(args, torch):
         m.set_state(st)
         m.autotune(reps=5)  # timed once for the grid, then the cached choice
     batch = M.Batch(members)
-    batch.step(max(args.warmup, 3))
+    batch.autotune(reps=3)
+    batch.step(max(warmup, 3))
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    t_batch = slowest_rank_seconds(_batch_time(batch, torch, args.steps))
+    t_batch = slowest_rank_seconds(_batch_time(batch, torch, steps))
     # sequential: the same members, one handle after another
     for m in members:
         m.step(1)
@@ -348,35 +407,34 @@ def run_ensemble(args, torch):
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for m in members:
-        m.step(args.steps)
+        m.step(steps)
     t_seq = slowest_rank_seconds(time.perf_counter() - t0)
-    if rank != 0:
-        return
     cells = 6 * N * N * total
-    rate = total * args.steps / t_batch
-    print(json.dumps({
-        "metric": f"ensemble member-steps/s ({args.members} x C96 per GPU, mixed lane)", "value": rate,
-        "unit": "member-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": max(args.warmup, 3),
-        "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (f64 metric transforms)", "data": "synthetic (seeded spherical harmonics)",
-        "config": {"workload": f"{total} members at C{N} ({args.members} per GPU, sharded by member), seed+k, "
-                               "RMS U[150,250] m, wind U[30,50] m/s, RK4, CFL 0.5",
-                   "l2": "inputs larger than L2 (all members' state)"},
-        "cell_steps_per_s": cells * args.steps / t_batch,
-        "sequential": {"value": total * args.steps / t_seq, "unit": "member-steps/s",
-                       "how": "each member's own handle (graph per step), one after another, host-timed"},
-        "batch_over_sequential": t_seq / t_batch,
-        "hbm": {"alg_GBs": ALG_BYTES_MIXED * cells * args.steps / t_batch / 1e9, "peak": _peaks()[0] * ws},
-    }))
+    launches, groups = batch.info()
+    alg = ALG_BYTES_MIXED * cells * steps / t_batch / 1e9
+    hbm = _peaks()[0] * ws
+    return {
+        "member_steps_per_s": total * steps / t_batch, "cell_steps_per_s": cells * steps / t_batch,
+        "members": total, "N": N, "steps": steps, "warmup": max(warmup, 3), "ms_per_step": 1e3 * t_batch / steps,
+        "sequential_member_steps_per_s": total * steps / t_seq, "batch_over_sequential": t_seq / t_batch,
+        "hbm_frac": alg / hbm, "alg_GBs": alg, "launches_per_stage": launches,
+        "tile_variant": groups[0][1] if groups else None,
+        "how": "one graph per step, one persistent launch per RK stage over all members' tiles, CUDA events on "
+               "the batch stream; sequential = each member's own handle (graph per step) one after another, "
+               "host-timed; inputs larger than L2",
+    }
 
 
-def run_uneven(args, torch):
+def run_uneven(torch, steps: int, warmup: int) -> dict:
     """16 x C48 + 8 x C96 + 4 x C192 + 1 x C384, per-instance CFL dt; one member of
-    each resolution below C384 on the FP64 lane, the others mixed."""
+    each resolution below C384 on the FP64 lane, the others mixed; one batch, one
+    launch per lane and RK stage, each lane's tile variant chosen by the batch
+    autotuner on its own work list.  Under torchrun every rank advances its own copy."""
     from conformal_cubed_sphere_gb300 import model as M
+    from conformal_cubed_sphere_gb300.parallel import slowest_rank_seconds
+    ws, rank, _ = _dist()
     groups = [(48, 16), (96, 8), (192, 4), (384, 1)]
     members, cells64, cells32, k = [], 0, 0, 0
-    variants = {}
     for N, cnt in groups:
         mesh = M.Mesh(N, HALO)
         for c in range(cnt):
@@ -385,8 +443,6 @@ def run_uneven(args, torch):
             dt = M.cfl_dt(mesh, st, 0.5)
             m = M.Stepper(mesh, dt, precision=lane, phi_mean=8000.0 * mesh.gravity)
             m.set_state(st)
-            m.autotune(reps=3)  # per resolution and lane (cached after the first member)
-            variants[f"C{N}_{lane}"] = "x".join(str(t) for t in m.variant[1:])
             members.append(m)
             if lane == "fp64":
                 cells64 += 6 * N * N
@@ -394,20 +450,24 @@ def run_uneven(args, torch):
                 cells32 += 6 * N * N
             k += 1
     batch = M.Batch(members)
-    batch.step(max(args.warmup, 3))
-    t = _batch_time(batch, torch, args.steps)
+    batch.autotune(reps=3)
+    batch.step(max(warmup, 3))
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    t = slowest_rank_seconds(_batch_time(batch, torch, steps))
     cells = cells64 + cells32
-    alg = (ALG_BYTES_FP64 * cells64 + ALG_BYTES_MIXED * cells32) * args.steps / t / 1e9
-    print(json.dumps({
-        "metric": "uneven batch cell-steps/s (16xC48 + 8xC96 + 4xC192 + 1xC384)", "value": cells * args.steps / t,
-        "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
-        "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 mixed + f64", "data": "synthetic (seeded spherical harmonics)",
-        "config": {"workload": "29 instances, per-instance CFL dt, one FP64 member per resolution below C384",
-                   "tiles": variants,
-                   "fp64_cells": cells64, "mixed_cells": cells32, "l2": "inputs larger than L2"},
-        "hbm": {"alg_GBs": alg, "peak": _peaks()[0], "frac": alg / _peaks()[0]},
-    }))
+    alg = (ALG_BYTES_FP64 * cells64 + ALG_BYTES_MIXED * cells32) * steps / t / 1e9
+    launches, info = batch.info()
+    tiles = {"fp64" if lane == 0 else "mixed": var for lane, var, _ in info}
+    return {
+        "cell_steps_per_s": ws * cells * steps / t, "steps": steps, "warmup": max(warmup, 3),
+        "ms_per_step": 1e3 * t / steps, "hbm_frac": ws * alg / (_peaks()[0] * ws), "alg_GBs": ws * alg,
+        "launches_per_stage": launches, "tile_variants": tiles, "fp64_cells": cells64, "mixed_cells": cells32,
+        "instances": len(members),
+        "how": "29 instances with per-instance CFL dt, one FP64 member per resolution below C384; one graph per "
+               "step, each lane's stages on its own stream; CUDA events on the batch stream",
+    }
 
 
 def main():
@@ -423,6 +483,7 @@ def main():
     ap.add_argument("--N", type=int, default=N_BENCH)
     ap.add_argument("--fp64-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batches", action="store_true", help="skip the ensemble and uneven measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -433,11 +494,33 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    batch_steps = max(5, min(args.steps, 50))
     if args.workload == "ensemble":
-        run_ensemble(args, torch)
+        e = run_ensemble(torch, args.members, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps({
+                "metric": f"ensemble member-steps/s ({args.members} x C96 per GPU, mixed lane)",
+                "value": e["member_steps_per_s"], "unit": "member-steps/s", "n_gpus": ws, "steps": e["steps"],
+                "warmup": e["warmup"], "ms_per_step": e["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 metric transforms)",
+                "data": "synthetic (seeded spherical harmonics)",
+                "config": {"workload": f"{e['members']} members at C96 ({args.members} per GPU, sharded by member), "
+                                       "seed+k, RMS U[150,250] m, wind U[30,50] m/s, RK4, CFL 0.5",
+                           "l2": "inputs larger than L2 (all members' state)"},
+                "ensemble": e}))
         return
     if args.workload == "uneven":
-        run_uneven(args, torch)
+        u = run_uneven(torch, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps({
+                "metric": "uneven batch cell-steps/s (16xC48 + 8xC96 + 4xC192 + 1xC384)",
+                "value": u["cell_steps_per_s"], "unit": "cell-steps/s", "n_gpus": ws, "steps": u["steps"],
+                "warmup": u["warmup"], "ms_per_step": u["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 mixed + f64",
+                "data": "synthetic (seeded spherical harmonics)",
+                "config": {"workload": "29 instances, per-instance CFL dt, one FP64 member per resolution below "
+                                       "C384", "l2": "inputs larger than L2"},
+                "uneven": u}))
         return
     from conformal_cubed_sphere_gb300 import model as M
 
@@ -468,13 +551,20 @@ def main():
     from conformal_cubed_sphere_gb300.parallel import slowest_rank_seconds
     t_mixed = slowest_rank_seconds(t_mixed)
     value = ws * cells * args.steps / t_mixed
+    ms_step = 1e3 * t_mixed / args.steps
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    counters = profiled_counters()
 
-    # roofline of the dominant kernel (the mixed stage kernel)
-    avg_ms, nl = kernel_launch_avg_ms(mixed, 4)
+    # roofline of the dominant kernel (the mixed stage kernel): a quarter of the timed
+    # step (events around each step's graph of four launches, so the launch gaps count
+    # against the kernel and 4 x kernel time equals the step time)
+    avg_ms = ms_step / 4.0
     hbm, peak_kind = _peaks()
     bytes_per_launch = ALG_BYTES_MIXED / 4.0 * cells
     achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
-    traffic = _traffic_per_launch(f"mixed_stage_C{mesh.N}")
+    prof_var = counters.get("mixed_variant", 0)
+    same_kernel = mesh.N == 384 and mixed.variant[0] == prof_var
+    traffic = counters.get("mixed_stage_C384") if same_kernel else None
 
     # FP64 parity lane on the same state
     f64 = M.Stepper(mesh, dt, precision="fp64", device=local)
@@ -484,7 +574,7 @@ def main():
     torch.cuda.synchronize()
     t_f64 = time_device_steps(f64, torch, args.fp64_steps, flush)
     fp64_value = cells * args.fp64_steps / t_f64
-    avg64_ms, _ = kernel_launch_avg_ms(f64, 1)
+    ms64 = 1e3 * t_f64 / args.fp64_steps
 
     # end to end through the C ABI
     e2e_steps = max(3, min(50, args.steps))
@@ -498,37 +588,48 @@ def main():
     e2e = ws * cells * e2e_steps / slowest_rank_seconds(el_async)
     e2e_sep = ws * cells * e2e_steps / slowest_rank_seconds(el_sep)
     e2e_sync = ws * cells * e2e_steps / slowest_rank_seconds(el_sync)
+    link = link_rates(torch, local, h2d, d2h)
+    link["link_bound_cell_steps_per_s"] = ws * cells / (link["link_both_ms"] * 1e-3)
+    for m in (mixed2,):
+        m.close()
+
+    ens = unv = None
+    if not args.no_batches:
+        ens = run_ensemble(torch, args.members, batch_steps, args.warmup)
+        unv = run_uneven(torch, batch_steps, args.warmup)
 
     if rank != 0:
         return
     clocks = sampler.summary()
     cpu = None if args.no_cpu else cpu_baseline(mesh, s, dt)
+    fp64_inst = counters.get("f64_stage_C384_fp64_thread_inst") if (
+        mesh.N == 384 and f64.variant[0] == counters.get("f64_variant", 1)) else None
     line = {
         "metric": "C384 cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_mixed / args.steps,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 metric transforms)",
         "data": "synthetic (seeded spherical harmonics)",
         "config": {"workload": f"C{mesh.N} seeded state with orography, RK4, CFL 0.5, mixed FP32/FP64 lane",
                    "N": mesh.N, "halo": HALO, "dt_s": dt, "l2": "flushed (256 MB write) between timed steps",
                    "parallelism": "replicas" if ws > 1 else "single",
                    "tile_variants": {lane: {"chosen": v, "launch_us": t} for lane, (v, t) in tuned.items()}},
-        "fp64_lane": {"value": fp64_value, "unit": "cell-steps/s", "ms_per_step": 1e3 * t_f64 / args.fp64_steps,
-                      "kernel_ms_avg": avg64_ms, "mixed_over_fp64": value / ws / fp64_value,
-                      "roofline": fp64_roofline(avg64_ms, _traffic_per_launch(f"f64_stage_C{mesh.N}_fp64_thread_inst")
-                                                if f64.variant[0] == 1 else None,  # the profiled 16x16 tile
-                                                torch.cuda.get_device_properties(local).multi_processor_count,
-                                                clocks)},
+        "fp64_lane": {"value": fp64_value, "unit": "cell-steps/s", "ms_per_step": ms64,
+                      "kernel_ms_avg": ms64 / 4.0, "mixed_over_fp64": value / ws / fp64_value,
+                      "over_cpu_baseline": (fp64_value / cpu["value"]) if cpu else None,
+                      "roofline": fp64_roofline(ms64 / 4.0, fp64_inst, sms, clocks)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": "mixed_stage_kernel", "kernel_ms_avg": avg_ms,
+                     "kernel_ms_how": "timed step / 4 (events around each step's graph of four launches)",
                      "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind,
-                     "issue": issue_roofline(avg_ms, _traffic_per_launch(f"mixed_stage_C{mesh.N}_warp_inst")
-                                             if mixed.variant[0] == 0 else None,  # the profiled 32x32 tile
-                                             torch.cuda.get_device_properties(local).multi_processor_count,
-                                             clocks)},
+                     "counters_sha16": counters.get("sources_sha16"),
+                     "issue": issue_roofline(avg_ms, counters.get("mixed_stage_C384_warp_inst") if same_kernel
+                                             else None, sms, clocks)},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "how": "ccs_set_state_async + ccs_step_async(1) + ccs_get_state_async per step, each state's "
                        "fields in one pinned host block (one copy per direction), one ccs_sync at the end",
-                "separate_field_arrays": e2e_sep, "synchronous_calls": e2e_sync},
+                "separate_field_arrays": e2e_sep, "synchronous_calls": e2e_sync, **link},
+        "ensemble": ens,
+        "uneven": unv,
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
         "cpu_baseline": cpu,

@@ -101,6 +101,10 @@ SIGNATURES = {
     "ccs_batch_step_async": (C.c_int, [_vp, C.c_int]),
     "ccs_batch_stream": (C.c_void_p, [_vp]),
     "ccs_batch_destroy": (None, [_vp]),
+    "ccs_batch_autotune": (C.c_int, [_vp, C.c_int]),
+    "ccs_batch_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int)]),
+    "ccs_batch_last_error": (C.c_char_p, [_vp]),
     "ccs_ghost_map": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     "ccs_timing": (C.c_int, [_vp, C.c_int, C.c_int, _dp, C.POINTER(C.c_int64)]),
     "ccs_stream": (C.c_void_p, [_vp]),

@@ -1347,7 +1347,7 @@ extern "C" int ccs_autotune(ccs_handle *h, int reps, int force, int *chosen, dou
 // batches: one launch per lane and RK stage over the union of the members' tiles
 // ---------------------------------------------------------------------------
 struct BatchGroup {
-  int lane = 0, n_rk = 0, nmem = 0, var = 0;
+  int lane = 0, scheme = 0, n_rk = 0, nmem = 0, var = 0;
   bool central = false;  // the members' spatial operator is a central difference
   bool ediss = false;    // the members reconstruct the E-flux dissipation
   std::vector<ccs_handle *> members;
@@ -1369,31 +1369,66 @@ struct ccs_batch {
   std::string err;
 };
 
+#define BATCH_TRY(b, call)                                                     \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      (b)->err = std::string(#call) + ": " + cudaGetErrorString(e_);           \
+      return CCS_ERR_CUDA;                                                     \
+    }                                                                          \
+  } while (0)
+
+static int group_nvar(const BatchGroup &g) { return g.lane == CCS_FP64 ? F64_NVAR : MX_NVAR; }
+
+// Stage k of group g (k = n_rk - 1 with with_sw: the FP64 final stage that also
+// writes the sphere winds) as one launch over the work list of all its members.
+static cudaError_t group_launch(BatchGroup &g, int k, bool with_sw) {
+  if (g.lane == CCS_FP64) {
+    const int row = (k == g.n_rk - 1 && with_sw) ? g.n_rk : k;
+    return launch_f64_stage(g.var, (const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork, g.grid,
+                            g.stream);
+  }
+  return launch_mixed_stage(g.var, g.central, g.ediss, (const MixedStage *)g.d_stages + (size_t)k * g.nmem,
+                            g.d_work, g.nwork, g.grid, g.stream);
+}
+
+// (Re)builds group g's work list for tile variant var: every tile of the six panels
+// of every member, member by member.
+static int group_set_var(ccs_batch *b, BatchGroup &g, int var) {
+  if (var < 0 || var >= group_nvar(g)) return CCS_ERR_ARG;
+  const TileShape ts = g.lane == CCS_FP64 ? kF64Tiles[var] : kMxTiles[var];
+  std::vector<WorkItem> work;
+  for (int m = 0; m < g.nmem; m++) {
+    const int N = g.members[m]->cfg.N;
+    const int ntx = (N + ts.tx - 1) / ts.tx, nty = (N + ts.ty - 1) / ts.ty;
+    for (int p = 0; p < 6; p++)
+      for (int ty = 0; ty < nty; ty++)
+        for (int tx = 0; tx < ntx; tx++)
+          work.push_back(WorkItem{(int16_t)m, (int16_t)p, (int16_t)tx, (int16_t)ty});
+  }
+  if (g.d_work) {
+    BATCH_TRY(b, cudaStreamSynchronize(g.stream));
+    BATCH_TRY(b, cudaFree(g.d_work));
+    g.d_work = nullptr;
+  }
+  BATCH_TRY(b, cudaMalloc(&g.d_work, work.size() * sizeof(WorkItem)));
+  BATCH_TRY(b, cudaMemcpy(g.d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+  g.nwork = (int)work.size();
+  g.var = var;
+  g.grid = g.lane == CCS_FP64 ? f64_max_grid(var, b->device) : mixed_max_grid(var, b->device);
+  return CCS_OK;
+}
+
 // One step of every group: the groups fork from the batch stream, run their RK
 // stages on their own streams (an FP64 group is FP64-issue bound and a mixed group
 // FP32 / latency bound, so they share the SMs well) and join back.
 static int batch_enqueue(ccs_batch *b, bool with_sw) {
-  if (cudaEventRecord(b->fork, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  BATCH_TRY(b, cudaEventRecord(b->fork, b->stream));
   for (auto &g : b->groups) {
-    if (cudaStreamWaitEvent(g.stream, b->fork, 0) != cudaSuccess) return CCS_ERR_CUDA;
-    for (int k = 0; k < g.n_rk; k++) {
-      cudaError_t e;
-      if (g.lane == CCS_FP64) {
-        const int row = (k == g.n_rk - 1 && with_sw) ? g.n_rk : k;
-        e = launch_f64_stage(g.var, (const F64Stage *)g.d_stages + (size_t)row * g.nmem, g.d_work, g.nwork,
-                             g.grid, g.stream);
-      } else {
-        e = launch_mixed_stage(g.var, g.central, g.ediss, (const MixedStage *)g.d_stages + (size_t)k * g.nmem,
-                               g.d_work, g.nwork,
-                               g.grid, g.stream);
-      }
-      if (e != cudaSuccess) {
-        b->err = cudaGetErrorString(e);
-        return CCS_ERR_CUDA;
-      }
-    }
-    if (cudaEventRecord(g.done, g.stream) != cudaSuccess) return CCS_ERR_CUDA;
-    if (cudaStreamWaitEvent(b->stream, g.done, 0) != cudaSuccess) return CCS_ERR_CUDA;
+    BATCH_TRY(b, cudaStreamWaitEvent(g.stream, b->fork, 0));
+    for (int k = 0; k < g.n_rk; k++) BATCH_TRY(b, group_launch(g, k, with_sw));
+    BATCH_TRY(b, cudaEventRecord(g.done, g.stream));
+    BATCH_TRY(b, cudaStreamWaitEvent(b->stream, g.done, 0));
   }
   return CCS_OK;
 }
@@ -1436,99 +1471,170 @@ extern "C" int ccs_debug_bounds_selftest(void) {
 #endif
 }
 
-extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out) {
-  if (!members || n < 1 || !out) return CCS_ERR_ARG;
-  *out = nullptr;
-  const int dev = members[0]->cfg.device;
-  for (int k = 0; k < n; k++) {
-    if (!members[k] || members[k]->cfg.device != dev) return CCS_ERR_ARG;
-    if (members[k]->cfg.precision == CCS_MIXED && !members[k]->mixed->have_phibar) return CCS_ERR_ARG;
-  }
-  if (n > 32767) return CCS_ERR_ARG;
-  cudaSetDevice(dev);
-  ccs_batch *b = new ccs_batch();
-  b->device = dev;
-  b->members.assign(members, members + n);
-  cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-  cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-  cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming);
+// Fills batch b (already holding its members): one group per (lane, scheme,
+// operator family, E-flux option), each with its own stream, stage table and work
+// list.  A group runs one tile variant for all its members: the variant of its
+// member with the most cells (that member's autotuned choice) until
+// ccs_batch_autotune times the group's own work list.
+static int batch_build(ccs_batch *b) {
+  const int n = (int)b->members.size();
+  BATCH_TRY(b, cudaSetDevice(b->device));
+  BATCH_TRY(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BATCH_TRY(b, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  BATCH_TRY(b, cudaEventCreateWithFlags(&b->after, cudaEventDisableTiming));
   auto member_var = [](const ccs_handle *m) { return m->cfg.precision == CCS_MIXED ? m->mixed->var : m->var; };
   for (int lane = 0; lane < 2; lane++)
     for (int scheme = 0; scheme < 2; scheme++)
-      for (int var = 0; var < (lane == CCS_FP64 ? F64_NVAR : MX_NVAR); var++)
-        for (int central = 0; central < 2; central++)
-          for (int ediss = 0; ediss < 2; ediss++) {
-      BatchGroup g;
-      g.lane = lane;
-      g.var = var;
-      g.central = central != 0;
-      g.ediss = ediss != 0;
-      for (int k = 0; k < n; k++)
-        if (members[k]->cfg.precision == lane && members[k]->cfg.scheme == scheme &&
-            member_var(members[k]) == var && (members[k]->op != CCS_OP_WENO) == g.central &&
-            (members[k]->cfg.e_dissipation != CCS_EDISS_ZERO) == g.ediss)
-          g.members.push_back(members[k]);
-      if (g.members.empty()) continue;
-      g.nmem = (int)g.members.size();
-      g.n_rk = scheme == CCS_RK4 ? 4 : 3;
-      cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
-      cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
-      std::vector<WorkItem> work;
-      const TileShape ts = lane == CCS_FP64 ? kF64Tiles[var] : kMxTiles[var];
-      const int TXg = ts.tx, TYg = ts.ty;
-      for (int m = 0; m < g.nmem; m++) {
-        const int N = g.members[m]->cfg.N;
-        const int ntx = (N + TXg - 1) / TXg, nty = (N + TYg - 1) / TYg;
-        for (int p = 0; p < 6; p++)
-          for (int ty = 0; ty < nty; ty++)
-            for (int tx = 0; tx < ntx; tx++)
-              work.push_back(WorkItem{(int16_t)m, (int16_t)p, (int16_t)tx, (int16_t)ty});
-      }
-      g.nwork = (int)work.size();
-      cudaMalloc(&g.d_work, work.size() * sizeof(WorkItem));
-      cudaMemcpy(g.d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice);
-      if (lane == CCS_FP64) {
-        std::vector<F64Stage> st((size_t)(g.n_rk + 1) * g.nmem);
-        for (int k = 0; k <= g.n_rk; k++)
-          for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->h_stages[k];
-        cudaMalloc(&g.d_stages, st.size() * sizeof(F64Stage));
-        cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(F64Stage), cudaMemcpyHostToDevice);
-        g.grid = f64_max_grid(var, dev);
-      } else {
-        std::vector<MixedStage> st((size_t)g.n_rk * g.nmem);
-        for (int k = 0; k < g.n_rk; k++)
-          for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->mixed->h_stages[k];
-        cudaMalloc(&g.d_stages, st.size() * sizeof(MixedStage));
-        cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(MixedStage), cudaMemcpyHostToDevice);
-        g.grid = mixed_max_grid(var, dev);
-      }
-      b->groups.push_back(g);
-    }
-  if (cudaGetLastError() != cudaSuccess) {
+      for (int central = 0; central < 2; central++)
+        for (int ediss = 0; ediss < 2; ediss++) {
+          std::vector<ccs_handle *> mem;
+          for (int k = 0; k < n; k++) {
+            ccs_handle *h = b->members[k];
+            if (h->cfg.precision == lane && h->cfg.scheme == scheme && (h->op != CCS_OP_WENO) == (central != 0) &&
+                (h->cfg.e_dissipation != CCS_EDISS_ZERO) == (ediss != 0))
+              mem.push_back(h);
+          }
+          if (mem.empty()) continue;
+          b->groups.emplace_back();  // owned by the batch from here on, so a failure below frees it
+          BatchGroup &g = b->groups.back();
+          g.lane = lane;
+          g.scheme = scheme;
+          g.central = central != 0;
+          g.ediss = ediss != 0;
+          g.members = mem;
+          g.nmem = (int)mem.size();
+          g.n_rk = scheme == CCS_RK4 ? 4 : 3;
+          BATCH_TRY(b, cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+          BATCH_TRY(b, cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+          ccs_handle *largest = mem[0];
+          for (ccs_handle *h : mem)
+            if (h->cfg.N > largest->cfg.N) largest = h;
+          int rc = group_set_var(b, g, member_var(largest));
+          if (rc) return rc;
+          if (lane == CCS_FP64) {
+            std::vector<F64Stage> st((size_t)(g.n_rk + 1) * g.nmem);
+            for (int k = 0; k <= g.n_rk; k++)
+              for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->h_stages[k];
+            BATCH_TRY(b, cudaMalloc(&g.d_stages, st.size() * sizeof(F64Stage)));
+            BATCH_TRY(b, cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(F64Stage), cudaMemcpyHostToDevice));
+          } else {
+            std::vector<MixedStage> st((size_t)g.n_rk * g.nmem);
+            for (int k = 0; k < g.n_rk; k++)
+              for (int m = 0; m < g.nmem; m++) st[(size_t)k * g.nmem + m] = g.members[m]->mixed->h_stages[k];
+            BATCH_TRY(b, cudaMalloc(&g.d_stages, st.size() * sizeof(MixedStage)));
+            BATCH_TRY(b, cudaMemcpy(g.d_stages, st.data(), st.size() * sizeof(MixedStage), cudaMemcpyHostToDevice));
+          }
+        }
+  return CCS_OK;
+}
+
+extern "C" int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out) {
+  if (!members || n < 1 || !out) return CCS_ERR_ARG;
+  *out = nullptr;
+  for (int k = 0; k < n; k++)
+    if (!members[k]) return CCS_ERR_ARG;
+  const int dev = members[0]->cfg.device;
+  for (int k = 0; k < n; k++) {
+    if (members[k]->cfg.device != dev) return CCS_ERR_ARG;
+    if (members[k]->cfg.precision == CCS_MIXED && !members[k]->mixed->have_phibar) return CCS_ERR_ARG;
+  }
+  if (n > 32767) return CCS_ERR_ARG;
+  ccs_batch *b = new ccs_batch();
+  b->device = dev;
+  b->members.assign(members, members + n);
+  const int rc = batch_build(b);
+  if (rc) {
     ccs_batch_destroy(b);
-    return CCS_ERR_CUDA;
+    return rc;
   }
   *out = b;
   return CCS_OK;
 }
 
+// Mean time of one stage launch of group g with its current variant: the stages
+// before the last, which read the members' states and write only stage scratch.
+static int group_time_stages(ccs_batch *b, BatchGroup &g, int reps, double *us) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  BATCH_TRY(b, cudaEventCreate(&e0));
+  cudaError_t e = cudaEventCreate(&e1);
+  const int nst = g.n_rk - 1;
+  if (e == cudaSuccess) e = group_launch(g, 0, false);  // warm-up
+  if (e == cudaSuccess) e = cudaEventRecord(e0, g.stream);
+  for (int r = 0; r < reps && e == cudaSuccess; r++)
+    for (int k = 0; k < nst && e == cudaSuccess; k++) e = group_launch(g, k, false);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, g.stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  BATCH_TRY(b, e);
+  *us = 1e3 * ms / (reps * nst);
+  return CCS_OK;
+}
+
+extern "C" int ccs_batch_autotune(ccs_batch *b, int reps) {
+  NvtxRange nvtx("ccs_batch_autotune");
+  if (!b || reps < 1) return CCS_ERR_ARG;
+  BATCH_TRY(b, cudaSetDevice(b->device));
+  for (ccs_handle *h : b->members) BATCH_TRY(b, cudaStreamSynchronize(h->stream));  // pending uploads
+  for (auto &g : b->groups) {
+    int best = -1;
+    double best_us = 0.;
+    for (int v = 0; v < group_nvar(g); v++) {
+      int rc = group_set_var(b, g, v);
+      if (rc) return rc;
+      double us = 0.;
+      rc = group_time_stages(b, g, reps, &us);
+      if (rc) return rc;
+      if (best < 0 || us < best_us) {
+        best = v;
+        best_us = us;
+      }
+    }
+    int rc = group_set_var(b, g, best);
+    if (rc) return rc;
+  }
+  if (b->g_step) cudaGraphExecDestroy(b->g_step);
+  if (b->g_step_sw) cudaGraphExecDestroy(b->g_step_sw);
+  b->g_step = b->g_step_sw = nullptr;
+  return CCS_OK;
+}
+
+extern "C" int ccs_batch_info(ccs_batch *b, int *launches_per_stage, int max_groups, int *lane, int *variant,
+                              int *members) {
+  if (!b || max_groups < 0) return CCS_ERR_ARG;
+  if (launches_per_stage) *launches_per_stage = (int)b->groups.size();
+  for (int q = 0; q < max_groups && q < (int)b->groups.size(); q++) {
+    const BatchGroup &g = b->groups[q];
+    if (lane) lane[q] = g.lane;
+    if (variant) variant[q] = g.var;
+    if (members) members[q] = g.nmem;
+  }
+  return CCS_OK;
+}
+
 static int batch_capture(ccs_batch *b, bool with_sw, cudaGraphExec_t *out) {
   cudaGraph_t g = nullptr;
-  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CCS_ERR_CUDA;
+  BATCH_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   int rc = batch_enqueue(b, with_sw);
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-  if (rc) return rc;
-  if (e != cudaSuccess) return CCS_ERR_CUDA;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  BATCH_TRY(b, e);
   e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
-  return e == cudaSuccess ? CCS_OK : CCS_ERR_CUDA;
+  BATCH_TRY(b, e);
+  return CCS_OK;
 }
 
 static int batch_step(ccs_batch *b, int nsteps, bool sync) {
   NvtxRange nvtx("ccs_batch_step");
   if (!b || nsteps < 0) return CCS_ERR_ARG;
   if (nsteps == 0) return CCS_OK;
-  cudaSetDevice(b->device);
+  BATCH_TRY(b, cudaSetDevice(b->device));
   if (!b->g_step) {
     int rc = batch_capture(b, false, &b->g_step);
     if (!rc) rc = batch_capture(b, true, &b->g_step_sw);
@@ -1537,18 +1643,15 @@ static int batch_step(ccs_batch *b, int nsteps, bool sync) {
   // the step starts after the members' own pending work (an asynchronous upload and
   // its import, an asynchronous step) and the members' later work after the step
   for (ccs_handle *h : b->members) {
-    if (!h->ev_order && cudaEventCreateWithFlags(&h->ev_order, cudaEventDisableTiming) != cudaSuccess)
-      return CCS_ERR_CUDA;
-    if (cudaEventRecord(h->ev_order, h->stream) != cudaSuccess) return CCS_ERR_CUDA;
-    if (cudaStreamWaitEvent(b->stream, h->ev_order, 0) != cudaSuccess) return CCS_ERR_CUDA;
+    if (!h->ev_order) BATCH_TRY(b, cudaEventCreateWithFlags(&h->ev_order, cudaEventDisableTiming));
+    BATCH_TRY(b, cudaEventRecord(h->ev_order, h->stream));
+    BATCH_TRY(b, cudaStreamWaitEvent(b->stream, h->ev_order, 0));
   }
-  for (int s = 0; s < nsteps - 1; s++)
-    if (cudaGraphLaunch(b->g_step, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
-  if (cudaGraphLaunch(b->g_step_sw, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
-  if (cudaEventRecord(b->after, b->stream) != cudaSuccess) return CCS_ERR_CUDA;
-  for (ccs_handle *h : b->members)
-    if (cudaStreamWaitEvent(h->stream, b->after, 0) != cudaSuccess) return CCS_ERR_CUDA;
-  if (sync && cudaStreamSynchronize(b->stream) != cudaSuccess) return CCS_ERR_CUDA;
+  for (int s = 0; s < nsteps - 1; s++) BATCH_TRY(b, cudaGraphLaunch(b->g_step, b->stream));
+  BATCH_TRY(b, cudaGraphLaunch(b->g_step_sw, b->stream));
+  BATCH_TRY(b, cudaEventRecord(b->after, b->stream));
+  for (ccs_handle *h : b->members) BATCH_TRY(b, cudaStreamWaitEvent(h->stream, b->after, 0));
+  if (sync) BATCH_TRY(b, cudaStreamSynchronize(b->stream));
   for (ccs_handle *h : b->members) h->sphere_valid = true;
   return CCS_OK;
 }
@@ -1556,6 +1659,7 @@ static int batch_step(ccs_batch *b, int nsteps, bool sync) {
 extern "C" int ccs_batch_step(ccs_batch *b, int nsteps) { return batch_step(b, nsteps, true); }
 extern "C" int ccs_batch_step_async(ccs_batch *b, int nsteps) { return batch_step(b, nsteps, false); }
 extern "C" void *ccs_batch_stream(ccs_batch *b) { return b ? (void *)b->stream : nullptr; }
+extern "C" const char *ccs_batch_last_error(const ccs_batch *b) { return b ? b->err.c_str() : ""; }
 
 extern "C" void ccs_batch_destroy(ccs_batch *b) {
   if (!b) return;

@@ -39,14 +39,20 @@ constexpr int NCELL_ARR = 11;
 // x / b for the constant divisors b = 3, 6, 12 of the reference (x/3., x/6.,
 // A*A*13./12.), correctly rounded: q0 = RN(x y) with y = RN(1/b), the remainder
 // r = x - q0 b is exact in one FMA, and q0 + r y rounded once is RN(x / b)
-// (Markstein's correction, IBM J. Res. Dev. 34(1), 1990).  A zero dividend keeps its
-// sign through q0.  The GPU test suite checks this against IEEE division.
+// (Markstein's correction, IBM J. Res. Dev. 34(1), 1990) when the quotient does not
+// underflow.  Where the correction does not apply, q0 is already the IEEE result: a
+// zero dividend keeps its sign, an infinite one stays infinite (the remainder would
+// be inf - inf = NaN) and a NaN stays NaN.  The GPU test suite checks this against
+// IEEE division.
 __device__ __forceinline__ double ccs_div_const(double x, double b, double y) {
   const double q0 = x * y;
   const double r = fma(-q0, b, x);
   const double q1 = fma(r, y, q0);
-  // x == +-0, tested on the bits: the FP64 pipe is the lane's bottleneck
-  return (__double_as_longlong(x) << 1) == 0 ? q0 : q1;
+  // x = +-0, +-inf or NaN, tested on the bits (the FP64 pipe is the lane's
+  // bottleneck): with the sign shifted out, 0 - 1 wraps to the top of the range and
+  // an all-ones exponent field is at least 0xffe0...
+  const unsigned long long t = (unsigned long long)__double_as_longlong(x) << 1;
+  return t - 1ull >= 0xffe0000000000000ull - 1ull ? q0 : q1;
 }
 
 namespace {

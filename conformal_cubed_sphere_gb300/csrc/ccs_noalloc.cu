@@ -1,12 +1,12 @@
 // ccs_noalloc.cu -- ccs_diag_noalloc: total mass and energy of a state that already
 // lives in device memory, for callers that must not allocate.
 //
-// Some host programs cannot call cudaMalloc: a driver that runs inside another
-// framework's memory pool or under a pre-sized device arena, or code that is being
-// captured into a CUDA graph where allocation is not allowed.  They own the state
-// on the device already and only want the diagnostic sums.  This entry point keeps
-// its only scratch -- one partial sum pair per panel row -- in the file-scope array
-// below, so it calls no cudaMalloc, cudaFree or allocating library routine.
+// Some host programs cannot call cudaMalloc: a model driver that runs inside another
+// framework's memory pool, or under a device arena sized once at start-up, must not
+// allocate behind that pool's back.  They hold the state on the device already and
+// only want the diagnostic sums.  This entry point keeps its only scratch -- one
+// partial sum pair per panel row -- in the file-scope array below, so it calls no
+// cudaMalloc, cudaFree or allocating library routine.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -19,7 +19,7 @@ namespace {
 // row, 6 * 4096 rows -> 384 KiB of device memory, held by every GPU that loads the
 // library until the process exits.
 constexpr int kMaxN = CCS_NOALLOC_MAX_N;
-__device__ __align__(256) double g_row_partials[2 * 6 * kMaxN];
+static __device__ __align__(256) double g_row_partials[2 * 6 * kMaxN];
 
 // Device addresses of g_row_partials, looked up once per device.
 constexpr int kMaxDevices = 64;
@@ -109,19 +109,44 @@ static int scratch_for_current_device(double **out) {
   return CCS_OK;
 }
 
+// Launches kernel `fn` and returns that launch's own status (cudaLaunchKernel
+// reports it directly, so an error left pending by unrelated earlier work of the
+// caller is neither returned as this call's failure nor cleared).  A failed launch's
+// error is taken back out of the runtime's last-error slot: it is reported through
+// the return code.
+static cudaError_t launch(const void *fn, dim3 grid, dim3 block, void **args, cudaStream_t s) {
+  const cudaError_t e = cudaLaunchKernel(fn, grid, block, args, 0, s);
+  if (e != cudaSuccess) cudaGetLastError();
+  return e;
+}
+
 extern "C" int ccs_diag_noalloc(int N, int halo, const double *phiG, const double *phi, const double *u,
                                 const double *v, const double *uC, const double *vC, const double *sqrtG,
                                 const double *phis, double *mass_energy, void *stream) {
   if (N < 1 || halo < 3 || !phiG || !phi || !u || !v || !uC || !vC || !sqrtG || !phis || !mass_energy)
     return CCS_ERR_ARG;
   if (N > kMaxN) return CCS_ERR_TOO_LARGE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CCS_ERR_CUDA;
+  if (s) {  // the scratch address below is the current device's: the stream must run there
+    int sdev = -1;
+    if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+      cudaGetLastError();
+      return CCS_ERR_ARG;
+    }
+    if (sdev != dev) return CCS_ERR_ARG;
+  }
   double *scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   // every partial the final sum reads is written earlier in the same call, so
   // nothing carries over from the previous call's contents
-  row_sums_kernel<<<6 * N, 256, 0, s>>>(N, halo, phiG, phi, u, v, uC, vC, sqrtG, phis, scratch);
-  final_sum_kernel<<<1, 256, 0, s>>>(6 * N, scratch, mass_energy);
-  return cudaGetLastError() == cudaSuccess ? CCS_OK : CCS_ERR_CUDA;
+  int n = N, h = halo, rows = 6 * N;
+  void *a1[] = {&n, &h, (void *)&phiG, (void *)&phi, (void *)&u, (void *)&v, (void *)&uC, (void *)&vC,
+                (void *)&sqrtG, (void *)&phis, &scratch};
+  if (launch((const void *)row_sums_kernel, dim3(6 * N), dim3(256), a1, s) != cudaSuccess) return CCS_ERR_CUDA;
+  void *a2[] = {&rows, &scratch, &mass_energy};
+  if (launch((const void *)final_sum_kernel, dim3(1), dim3(256), a2, s) != cudaSuccess) return CCS_ERR_CUDA;
+  return CCS_OK;
 }

@@ -204,8 +204,16 @@ bool parse(int argc, char **argv, Options &o) {
       if (dom.count("xhalo")) o.halo = std::atoi(dom["xhalo"].c_str());
       if (dom.count("mesh_file")) {
         const std::string mf = trim(dom["mesh_file"]);
-        if (file_exists(mf)) o.mesh_file = mf;
-        else std::fprintf(stderr, "ccsm_gpu: mesh_file '%s' not found: the mesh is generated\n", mf.c_str());
+        int fn = 0, fmap = 0;
+        // the reference's own mesh_file is NetCDF (io_mod.F90:37): only a raw-binary
+        // mesh file is read, anything else leaves the mesh to the generator
+        if (!file_exists(mf))
+          std::fprintf(stderr, "ccsm_gpu: mesh_file '%s' not found: the mesh is generated\n", mf.c_str());
+        else if (ccs_mesh_file_info(mf.c_str(), &fn, &fmap) != CCS_OK)
+          std::fprintf(stderr, "ccsm_gpu: mesh_file '%s' is not a raw-binary mesh file: the mesh is generated\n",
+                       mf.c_str());
+        else
+          o.mesh_file = mf;
       }
     } else if (a == "--mesh-namelist") {
       const std::string path = val("--mesh-namelist");

@@ -254,6 +254,17 @@ def history_writer(prefix: str, mesh) -> Callable:
     return write
 
 
+def is_raw_mesh_file(path) -> bool:
+    """Whether `path` is a raw-binary mesh file (ccs_mesh_file_info).  The reference's
+    own mesh_file is NetCDF (io_mod.F90:37), which cannot be read here: the drivers
+    then generate the mesh instead."""
+    import ctypes as C
+
+    from . import _lib as L
+    fn, fmap = C.c_int(), C.c_int()
+    return L.lib().ccs_mesh_file_info(str(path).encode(), C.byref(fn), C.byref(fmap)) == L.CCS_OK
+
+
 def main(argv=None) -> int:
     """The model program (ccsm.F90) from the reference's namelist files, on the GPU:
     python -m conformal_cubed_sphere_gb300.driver --namelist namelist.input
@@ -280,7 +291,12 @@ def main(argv=None) -> int:
     if rs.time.integral_scheme not in ("RK4", "RK3_TVD"):
         print(f"unknown integral scheme {rs.time.integral_scheme}")  # parameters_mod.F90:146
         return 2
+    raw_mesh = False
     if rs.mesh_file and os.path.exists(rs.mesh_file):
+        raw_mesh = is_raw_mesh_file(rs.mesh_file)
+        if not raw_mesh:
+            print(f" mesh_file {rs.mesh_file} is not a raw-binary mesh file: the mesh is generated")
+    if raw_mesh:
         mesh = M.Mesh.from_file(rs.mesh_file, halo=rs.halo, radius=a.radius)
     else:
         N = a.N or (mesh_resolution_from_namelist(a.mesh_namelist) if a.mesh_namelist else None)

@@ -343,7 +343,8 @@ class Stepper:
 
 
 class Batch:
-    """Members advanced together: one launch per lane and RK stage."""
+    """Members advanced together: one launch per group (lane, RK scheme, operator
+    family, E-flux option) and RK stage."""
 
     def __init__(self, members: list[Stepper]):
         self.members = members
@@ -352,11 +353,28 @@ class Batch:
         L.check(L.lib().ccs_batch_create(arr, len(members), C.byref(b)), "ccs_batch_create")
         self.handle = b
 
+    def _check(self, status: int, where: str):
+        if status != L.CCS_OK:
+            raise L.CCSError(status, where, (L.lib().ccs_batch_last_error(self.handle) or b"").decode())
+
     def step(self, nsteps: int = 1):
-        L.check(L.lib().ccs_batch_step(self.handle, int(nsteps)), "ccs_batch_step")
+        self._check(L.lib().ccs_batch_step(self.handle, int(nsteps)), "ccs_batch_step")
 
     def step_async(self, nsteps: int = 1):
-        L.check(L.lib().ccs_batch_step_async(self.handle, int(nsteps)), "ccs_batch_step_async")
+        self._check(L.lib().ccs_batch_step_async(self.handle, int(nsteps)), "ccs_batch_step_async")
+
+    def autotune(self, reps: int = 3):
+        """Times each group's tile variants on its own work list and keeps the fastest
+        (ccs_batch_autotune)."""
+        self._check(L.lib().ccs_batch_autotune(self.handle, int(reps)), "ccs_batch_autotune")
+
+    def info(self):
+        """(launches per RK stage, [(lane, tile variant, members) per group])."""
+        n = C.c_int()
+        L.check(L.lib().ccs_batch_info(self.handle, C.byref(n), 0, None, None, None), "ccs_batch_info")
+        lane, var, mem = (C.c_int * n.value)(), (C.c_int * n.value)(), (C.c_int * n.value)()
+        L.check(L.lib().ccs_batch_info(self.handle, C.byref(n), n.value, lane, var, mem), "ccs_batch_info")
+        return n.value, [(lane[q], var[q], mem[q]) for q in range(n.value)]
 
     @property
     def stream_ptr(self) -> int:

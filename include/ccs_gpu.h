@@ -214,12 +214,14 @@ int ccs_diag(ccs_handle *h, double *total_mass, double *total_energy);
 
 /* Total mass and energy, like ccs_diag, of a state that already lives in device
  * memory, without allocating anything.  This entry point has no counterpart in the
- * reference.  It serves callers that cannot call cudaMalloc (code running inside
- * another framework's memory pool or a fixed device arena, or being captured into
- * a CUDA graph).  All array arguments are device pointers in the reference layout
- * (ics:ice, jcs:jce, 6); mass_energy is a device pointer to two doubles; stream is a
- * cudaStream_t (NULL for the legacy default stream) and the call returns once the
- * work is enqueued.  Its scratch is a fixed device array sized for N up to
+ * reference.  It serves callers that cannot call cudaMalloc: a model driver that
+ * runs inside another framework's memory pool, or under a device arena sized once
+ * at start-up, must not allocate behind that pool's back.  All array arguments are
+ * device pointers in the reference layout (ics:ice, jcs:jce, 6); mass_energy is a
+ * device pointer to two doubles; stream is a cudaStream_t of the current device
+ * (NULL for the legacy default stream; a stream of another device returns
+ * CCS_ERR_ARG) and the call returns once the work is enqueued, with the status of
+ * its own launches only.  Its scratch is a fixed device array sized for N up to
  * CCS_NOALLOC_MAX_N (larger N returns CCS_ERR_TOO_LARGE); every GPU that loads the
  * library holds that array until exit.  The first call on a device looks up the
  * array's device address, so make it before any stream capture.  All calls share
@@ -232,18 +234,35 @@ int ccs_diag_noalloc(int N, int halo, const double *phiG, const double *phi, con
 /* ---- ensembles and uneven batches ---------------------------------------- */
 
 /* Groups handles (any mix of N, dt and lanes) so that each RK stage of all members
- * runs as one launch per lane over a shared work list, captured in a CUDA graph.
- * A batch step is ordered after each member's pending work on its own stream (an
- * asynchronous upload and its import, an asynchronous step), and each member's later
- * work after the batch step, so the members' *_async calls and ccs_batch_step_async
- * compose in call order.  The batch keeps each member's tile variant and operator
- * as they were at creation, and the members must outlive it (ccs_batch_destroy
- * first). */
+ * runs as one launch per group over a shared work list, captured in a CUDA graph.
+ * The members of a group share the lane, the RK scheme, the operator family (WENO-Z
+ * or central differences) and the E-flux option: an ensemble, or an uneven mix of
+ * resolutions on both lanes, runs one launch per lane and RK stage.  A group runs
+ * one tile variant for all its members, at first the variant of its member with the
+ * most cells (tune members before creating the batch), or the one
+ * ccs_batch_autotune picks by timing the group's own work list.  A batch step is
+ * ordered after each member's pending work on its own stream (an asynchronous
+ * upload and its import, an asynchronous step), and each member's later work after
+ * the batch step, so the members' *_async calls and ccs_batch_step_async compose in
+ * call order.  The batch keeps each member's operator as it was at creation, and
+ * the members must outlive it (ccs_batch_destroy first).  The reference advances
+ * one grid per program run (ccsm.F90:50-67); batches have no counterpart there. */
 int ccs_batch_create(ccs_handle *const *members, int n, ccs_batch **out);
 int ccs_batch_step(ccs_batch *b, int nsteps);
 /* Same, enqueued on the batch's stream (ccs_batch_stream) without waiting. */
 int ccs_batch_step_async(ccs_batch *b, int nsteps);
 void *ccs_batch_stream(ccs_batch *b);
+/* Times every tile variant of each group on the group's work list (the RK stages
+ * before the last, which leave the members' states unchanged; `reps` rounds after
+ * one warm-up launch) and keeps the fastest per group.  Results do not depend on
+ * the variant. */
+int ccs_batch_autotune(ccs_batch *b, int reps);
+/* launches_per_stage (may be NULL): the number of groups, one launch each per RK
+ * stage; for the first max_groups groups, lane (CCS_FP64 / CCS_MIXED), tile variant
+ * and member count (each array may be NULL). */
+int ccs_batch_info(ccs_batch *b, int *launches_per_stage, int max_groups, int *lane, int *variant, int *members);
+/* Text of the last CUDA error a batch call met ("" if none). */
+const char *ccs_batch_last_error(const ccs_batch *b);
 void ccs_batch_destroy(ccs_batch *b);
 
 /* ---- introspection -------------------------------------------------------- */

@@ -1,5 +1,6 @@
 """Writes golden.json: SHA-256 digests (and a few values) of the oracle's results on
-small seeded cases, plus digests of the host generator's mesh and initial state.
+small seeded cases, plus digests of the host generator's mesh and initial state, and
+golden_inputs.npz: every case's mesh and initial state as arrays.
 
 The reference has no tests, fixtures or golden vectors and cannot be built here
 (Fortran + NetCDF), so these fixtures are the oracle's own results: they pin the
@@ -78,16 +79,17 @@ def main():
         out["cases"][name] = rec
     (HERE / "golden.json").write_text(json.dumps(out, indent=1) + "\n")
     print("wrote", HERE / "golden.json")
-    # the first case's inputs as arrays, so that a machine whose libm rounds the
+    # every case's inputs as arrays, so that a machine whose libm rounds the
     # generator's sin/cos/atan2 differently still steps exactly these inputs
-    name, N, halo, ic, scheme, ediss, op, steps = CASES[0]
-    mesh, s, dt = case_inputs(N, halo, ic)
-    arrays = {f"mesh_{k}": getattr(mesh, k) for k in MESH_FIELDS}
-    arrays.update({f"state_{k}": s[k] for k in M.STATE_FIELDS})
-    arrays["scalars"] = np.array([N, halo, mesh.dx, mesh.dy, dt, mesh.radius, mesh.gravity, mesh.omega])
-    np.savez_compressed(HERE / f"{name}_inputs.npz", **arrays)
-    print("wrote", HERE / f"{name}_inputs.npz")
-
+    arrays = {}
+    for name, N, halo, ic, scheme, ediss, op, steps in CASES:
+        mesh, s, dt = case_inputs(N, halo, ic)
+        arrays.update({f"{name}/mesh_{k}": getattr(mesh, k) for k in MESH_FIELDS})
+        arrays.update({f"{name}/state_{k}": s[k] for k in FIELDS})
+        arrays[f"{name}/scalars"] = np.array([N, halo, mesh.dx, mesh.dy, dt, mesh.radius, mesh.gravity,
+                                              mesh.omega])
+    np.savez_compressed(HERE / "golden_inputs.npz", **arrays)
+    print("wrote", HERE / "golden_inputs.npz")
 
 if __name__ == "__main__":
     main()

@@ -30,6 +30,30 @@ def test_reference_arm_prints_one_contract_line():
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
 
 
+def test_reference_arm_maps_no_cuda_library():
+    """The reference arm makes its inputs with the CPU-only set-up library: the
+    process that times the oracle never maps libccs_gpu.so."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '1']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPPED', int('libccs_gpu' in maps), int('libccs_setup' in maps), int('libccs_oracle' in maps))")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    tail = [ln for ln in r.stdout.splitlines() if ln.startswith("MAPPED")]
+    assert tail == ["MAPPED 0 1 1"], r.stdout[-2000:]
+
+
+def test_kernel_counters_are_tied_to_the_sources():
+    """bench.py uses the committed ncu counters only for the kernel sources they were
+    taken on."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    h = bench.kernel_sources_hash()
+    assert len(h) == 16
+    d = json.loads((ROOT / "profiles" / "roofline_traffic.json").read_text())
+    assert bench.profiled_counters() == (d if d.get("sources_sha16") == h else {})
+
+
 def test_issue_roofline():
     sys.path.insert(0, str(ROOT))
     import bench

@@ -386,3 +386,23 @@ def test_python_driver_cli_needs_a_mesh(tmp_path):
     nl.write_text(_NAMELIST)
     with pytest.raises(SystemExit):
         D.main(["--namelist", str(nl)])
+
+
+def test_a_netcdf_mesh_file_is_not_read_as_raw(tmp_path):
+    """The reference's mesh_file is NetCDF: both drivers probe it and generate the
+    mesh instead of failing on it; a raw-binary mesh file is recognised."""
+    import subprocess
+
+    from conformal_cubed_sphere_gb300 import model as M
+    nc = tmp_path / "ccs_mesh.nc"
+    nc.write_bytes(b"CDF\x01" + bytes(4096))  # a NetCDF classic header, not a raw-binary mesh
+    assert not D.is_raw_mesh_file(nc)
+    raw = tmp_path / "mesh.ccsmesh"
+    M.Mesh(6, 3).save(raw)
+    assert D.is_raw_mesh_file(raw)
+    nl = tmp_path / "namelist.input"
+    nl.write_text(_NAMELIST.replace("no/such/mesh!file", str(nc)))
+    r = subprocess.run([_driver_binary(), "--namelist", str(nl), "--N", "12", "--plan"],
+                       capture_output=True, text=True, check=True)
+    assert f"mesh_file '{nc}' is not a raw-binary mesh file: the mesh is generated" in r.stderr
+    assert " N 12 halo 4 " in r.stdout

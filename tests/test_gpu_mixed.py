@@ -101,6 +101,7 @@ def test_uneven_batch_mixed_lanes():
         b.set_state(st)
         ref.append(b)
     batch = M.Batch(members)
+    assert batch.info()[0] == 2  # one launch per lane and RK stage
     batch.step(3)
     for a, b in zip(members, ref):
         b.step(3)

@@ -1,6 +1,6 @@
 """Tile variants of the stage kernels and the autotuner: every variant gives the
 same bits (FP64 lane: the oracle's), the autotuner leaves the state unchanged and
-caches its choice, and batches group members by variant."""
+caches its choice, and batches run one variant per lane group."""
 import numpy as np
 import pytest
 
@@ -77,28 +77,42 @@ def test_autotune_keeps_state_and_caches(precision):
         assert bitwise_equal(a[k], b[k], m), k
 
 
-def test_batch_groups_members_by_variant():
+def test_batch_runs_one_launch_per_lane_whatever_the_members_variants():
+    """Members tuned to different tile variants share one launch per lane and RK
+    stage (the group runs one variant for all); ccs_batch_autotune re-picks each
+    group's variant by timing its work list; every member equals its single run bit
+    for bit before and after."""
     mesh, s, dt = seeded_case(20, 3, seed=8, oro=True)
-    members, singles = [], []
+    kw = dict(phi_mean=8000.0 * mesh.gravity)
+    members, lanes = [], []
     for var in (0, 1, 2):
         x = M.Stepper(mesh, dt, precision="fp64")
         x.set_variant(var)
         x.set_state(s)
         members.append(x)
-    y = M.Stepper(mesh, dt, precision="mixed", phi_mean=8000.0 * mesh.gravity)
-    y.set_variant(1)
-    y.set_state(s)
-    members.append(y)
-    M.Batch(members).step(2)
-    for x in members:
-        r = M.Stepper(mesh, dt, precision="fp64" if x is not y else "mixed",
-                      **({} if x is not y else dict(phi_mean=8000.0 * mesh.gravity)))
+        lanes.append("fp64")
+    for var in (1, 0):
+        y = M.Stepper(mesh, dt, precision="mixed", **kw)
+        y.set_variant(var)
+        y.set_state(s)
+        members.append(y)
+        lanes.append("mixed")
+    b = M.Batch(members)
+    launches, groups = b.info()
+    assert launches == 2
+    assert sorted((lane, n) for lane, _, n in groups) == [(L.CCS_FP64, 3), (L.CCS_MIXED, 2)]
+    b.step(1)
+    b.autotune(reps=2)
+    assert b.info()[0] == 2
+    b.step(1)
+    m = valid_mask(mesh)
+    for x, lane in zip(members, lanes):
+        r = M.Stepper(mesh, dt, precision=lane, **(kw if lane == "mixed" else {}))
         r.set_state(s)
         r.step(2)
-        a, b = x.get_state(), r.get_state()
-        m = valid_mask(mesh)
+        a, c = x.get_state(), r.get_state()
         for k in CHECK_FIELDS:
-            assert bitwise_equal(a[k], b[k], m), k
+            assert bitwise_equal(a[k], c[k], m), (lane, k)
 
 
 def test_batch_groups_mixed_members_by_operator():

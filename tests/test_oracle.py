@@ -313,3 +313,25 @@ def test_pole_inverse_option_inverts_a_at_the_poles():
     assert np.array_equal(ref.matrixIA[keep], fix.matrixIA[keep])
     s = M.initial_state(fix, kind=L.CCS_IC_SEEDED, seed=4, lmax_oro=8)
     assert np.max(np.abs(s["u"][~fix.corner_mask()])) < 1e12
+
+
+# ---- initTestCase's conversion (test_case_mod.F90:38-48) ----------------------
+
+@pytest.mark.parametrize("N,halo", [(8, 3), (20, 4), (33, 5)])
+@pytest.mark.parametrize("kind", [L.CCS_IC_CASE2, L.CCS_IC_CASE5, L.CCS_IC_CASE6, L.CCS_IC_SEEDED])
+def test_state_from_sphere_matches_oracle_bitwise(N, halo, kind):
+    """phiG = phi sqrtG, (u, v) = G IA (zonal, meridional), (uC, vC) = IA (zonal,
+    meridional) over the whole array.  The product's ccs_state_from_sphere, which
+    makes the initial state of every parity test, equals the oracle's restatement
+    bit for bit (corner blocks included)."""
+    mesh = M.Mesh(N, halo)
+    s = M.initial_state(mesh, kind=kind, seed=5, lmax_oro=8)
+    orc = O.Oracle.from_mesh(mesh)
+    given = {k: np.full(mesh.ncell, np.nan) for k in O.FIELDS}
+    for k in ("phi", "zonal_wind", "meridional_wind"):
+        given[k] = s[k]
+    orc.set_state(given)
+    orc.init_from_sphere(0)
+    o = orc.get_state()
+    for k in ("phiG", "u", "v", "uC", "vC"):
+        assert np.array_equal(s[k].view(np.int64), o[k].view(np.int64)), k

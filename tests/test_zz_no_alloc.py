@@ -1,11 +1,12 @@
 """ccs_diag_noalloc: the diagnostics for callers that cannot allocate device memory.
 
-Programs running inside another framework's memory pool, under a fixed device
-arena, or inside a CUDA graph capture cannot call cudaMalloc; they hold the state
-in device memory already.  This test gives the entry point device buffers it did
-not allocate (the test allocates them through torch), calls it twice in a row
-through the C ABI, and checks both results against ccs_diag of the same state
-through a normal handle.  It sits in its own file, collected last.
+A model driver that runs inside another framework's memory pool, or under a device
+arena sized once at start-up, must not call cudaMalloc; it holds the state in device
+memory already.  This test gives the entry point device buffers it did not allocate
+(the test allocates them through torch), calls it twice in a row through the C ABI,
+and checks both results against ccs_diag of the same state through a normal handle;
+a further call after those must leave the device's free memory unchanged.  It sits
+in its own file, collected last.
 """
 import ctypes as C
 
@@ -44,6 +45,17 @@ def test_diag_noalloc_matches_diag_twice():
         assert m2 == pytest.approx(mass, rel=1e-13)
         assert e2 == pytest.approx(energy, rel=1e-13)
         out.fill_(float("nan"))
+
+    # a call after the first ones allocates nothing: the device's free memory stays
+    torch.cuda.synchronize(dev)
+    free0, _ = torch.cuda.mem_get_info(dev)
+    rc = lib.ccs_diag_noalloc(mesh.N, mesh.halo, *[t.data_ptr() for t in d], out.data_ptr(), stream)
+    assert rc == L.CCS_OK
+    torch.cuda.synchronize(dev)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0
+    m3, e3 = out.cpu().tolist()
+    assert m3 == pytest.approx(mass, rel=1e-13) and e3 == pytest.approx(energy, rel=1e-13)
 
     # above the fixed scratch capacity the call is rejected before any launch
     big = L.CCS_NOALLOC_MAX_N + 1
