@@ -265,10 +265,11 @@ def e2e_rate(stepper, mesh, state, steps: int, torch):
     return el_async, el_sep, el_sync, n_in * nb, n_out * nb
 
 
-def link_rates(torch, dev: int, h2d_bytes: int, d2h_bytes: int, reps: int = 5) -> dict:
-    """The host link alone, for one step's bytes: one pinned upload of h2d_bytes, one
-    pinned download of d2h_bytes, and both at once on two streams; CUDA events, best
-    of `reps` after a warm-up round.  The e2e loop cannot beat `both_ms` per step."""
+def link_rates(torch, dev: int, h2d_bytes: int, d2h_bytes: int, reps: int = 10) -> dict:
+    """The host link alone, for one step's bytes: `reps` pinned uploads of h2d_bytes
+    back to back, `reps` pinned downloads of d2h_bytes, and both streams at once (the
+    e2e loop's pattern); CUDA events around each run after a warm-up run, per copy.
+    The e2e loop cannot move its bytes faster than `both_ms` per step."""
     hin = torch.empty(h2d_bytes, dtype=torch.uint8).pin_memory()
     hout = torch.empty(d2h_bytes, dtype=torch.uint8).pin_memory()
     din = torch.empty(h2d_bytes, dtype=torch.uint8, device=dev)
@@ -276,30 +277,30 @@ def link_rates(torch, dev: int, h2d_bytes: int, d2h_bytes: int, reps: int = 5) -
     s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
 
     def timed(up: bool, down: bool) -> float:
-        best = None
-        for r in range(reps + 1):
+        ms = 0.0
+        for r in range(2):  # the first run warms up
             torch.cuda.synchronize(dev)
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record(s_up)
             s_down.wait_event(e0)
-            if up:
-                with torch.cuda.stream(s_up):
-                    din.copy_(hin, non_blocking=True)
-            if down:
-                with torch.cuda.stream(s_down):
-                    hout.copy_(dout, non_blocking=True)
+            for _ in range(reps):
+                if up:
+                    with torch.cuda.stream(s_up):
+                        din.copy_(hin, non_blocking=True)
+                if down:
+                    with torch.cuda.stream(s_down):
+                        hout.copy_(dout, non_blocking=True)
             e1.record(s_up)
             e2.record(s_down)
             torch.cuda.synchronize(dev)
-            ms = max(e0.elapsed_time(e1), e0.elapsed_time(e2))
-            if r > 0 and (best is None or ms < best):
-                best = ms
-        return best
+            ms = max(e0.elapsed_time(e1), e0.elapsed_time(e2)) / reps
+        return ms
 
     t_up, t_down, t_both = timed(True, False), timed(False, True), timed(True, True)
     return {"link_h2d_gbs": h2d_bytes / t_up / 1e6, "link_d2h_gbs": d2h_bytes / t_down / 1e6,
-            "link_both_ms": t_both, "how": "one pinned copy per direction of the e2e step's bytes, CUDA events, "
-                                           "best of %d; both = the two copies at once on two streams" % reps}
+            "link_both_ms": t_both, "link_how": "%d pinned copies of the e2e step's bytes back to back per "
+                                               "direction, CUDA events, per copy; both = the two directions at "
+                                               "once on two streams" % reps}
 
 
 def cpu_baseline(mesh, state, dt, seconds=10.0):

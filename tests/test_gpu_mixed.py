@@ -43,14 +43,15 @@ def test_short_horizon_error_vs_fp64(oro):
 
 def test_error_within_the_fp64_divergence_floor():
     """Over 200 steps the WENO branch switches make any non-bitwise run diverge;
-    the mixed lane's h error stays within a small factor of the FP64 lane perturbed
-    by one FP32 ulp (6e-8) in phiG."""
+    the mixed lane's h error stays within 2x the divergence of the FP64 lane perturbed
+    by one FP32 ulp (6e-8) in phiG (measured ratios 0.9-1.35 at steps 100 and 200 on
+    seeds 2 and 3)."""
     from conformal_cubed_sphere_gb300 import accuracy as A
     res = A.run(N=32, days=10.0, checkpoints=2, seed=2, oro=True, floor=True, floor_eps=6e-8, max_steps=200)
     for row in res["checkpoints"]:
         mixed = row["mixed_vs_fp64"]["h"]["L2"]
         floor = row["fp64_perturbed_vs_fp64"]["h"]["L2"]
-        assert mixed < max(20 * floor, 1e-6), row
+        assert mixed < 2 * floor, row
 
 
 def test_mass_drift_small():
