@@ -359,6 +359,16 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def variant_name(lane: str, var: int) -> str:
+    """A stage-kernel variant as "<tile> <halo-staging schedule>" (mixed lane) or
+    "<tile>" (FP64 lane)."""
+    from conformal_cubed_sphere_gb300 import _lib as L
+    if lane == "mixed":
+        tx, ty, staging = L.MIXED_VARIANTS[var]
+        return f"{tx}x{ty} {staging}"
+    return ("32x8", "16x16", "64x4")[var]
+
+
 def _batch_time(batch, torch, steps: int):
     st = torch.cuda.ExternalStream(batch.stream_ptr)
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -420,6 +430,7 @@ def run_ensemble(torch, members_per_gpu: int, steps: int, warmup: int) -> dict:
         "sequential_member_steps_per_s": total * steps / t_seq, "batch_over_sequential": t_seq / t_batch,
         "hbm_frac": alg / hbm, "alg_GBs": alg, "launches_per_stage": launches,
         "tile_variant": groups[0][1] if groups else None,
+        "variant": variant_name("mixed", groups[0][1]) if groups else None,
         "how": "one graph per step, one persistent launch per RK stage over all members' tiles, CUDA events on "
                "the batch stream; sequential = each member's own handle (graph per step) one after another, "
                "host-timed; inputs larger than L2",
@@ -461,10 +472,12 @@ def run_uneven(torch, steps: int, warmup: int) -> dict:
     alg = (ALG_BYTES_FP64 * cells64 + ALG_BYTES_MIXED * cells32) * steps / t / 1e9
     launches, info = batch.info()
     tiles = {"fp64" if lane == 0 else "mixed": var for lane, var, _ in info}
+    names = {k: variant_name(k, v) for k, v in tiles.items()}
     return {
         "cell_steps_per_s": ws * cells * steps / t, "steps": steps, "warmup": max(warmup, 3),
         "ms_per_step": 1e3 * t / steps, "hbm_frac": ws * alg / (_peaks()[0] * ws), "alg_GBs": ws * alg,
-        "launches_per_stage": launches, "tile_variants": tiles, "fp64_cells": cells64, "mixed_cells": cells32,
+        "launches_per_stage": launches, "tile_variants": tiles, "variants": names, "fp64_cells": cells64,
+        "mixed_cells": cells32,
         "instances": len(members),
         "how": "29 instances with per-instance CFL dt, one FP64 member per resolution below C384; one graph per "
                "step, each lane's stages on its own stream; CUDA events on the batch stream",
@@ -613,7 +626,8 @@ def main():
         "config": {"workload": f"C{mesh.N} seeded state with orography, RK4, CFL 0.5, mixed FP32/FP64 lane",
                    "N": mesh.N, "halo": HALO, "dt_s": dt, "l2": "flushed (256 MB write) between timed steps",
                    "parallelism": "replicas" if ws > 1 else "single",
-                   "tile_variants": {lane: {"chosen": v, "launch_us": t} for lane, (v, t) in tuned.items()}},
+                   "tile_variants": {lane: {"chosen": v, "variant": variant_name(lane, v), "launch_us": t}
+                                     for lane, (v, t) in tuned.items()}},
         "fp64_lane": {"value": fp64_value, "unit": "cell-steps/s", "ms_per_step": ms64,
                       "kernel_ms_avg": ms64 / 4.0, "mixed_over_fp64": value / ws / fp64_value,
                       "over_cpu_baseline": (fp64_value / cpu["value"]) if cpu else None,

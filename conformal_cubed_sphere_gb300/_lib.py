@@ -33,6 +33,8 @@ CCS_MIXED = 1
 CCS_EDISS_ZERO = 0
 CCS_EDISS_RECONSTRUCT = 1
 CCS_MAX_VARIANTS = 4
+# mixed-lane variants: (tile_x, tile_y, halo-staging schedule)
+MIXED_VARIANTS = ((32, 32, "loads"), (32, 16, "loads"), (32, 32, "async"), (32, 16, "async"))
 CCS_OP_WENO, CCS_OP_CENTRAL2, CCS_OP_CENTRAL4, CCS_OP_CENTRAL6 = 0, 2, 4, 6
 CCS_MAP_GNOMONIC_EQUIANGULAR = 0
 CCS_MAP_CONFORMAL = 1

@@ -86,8 +86,15 @@ struct TileShape {
 };
 constexpr int F64_NVAR = 3;  // 32 x 8, 16 x 16, 64 x 4 (256 threads, one cell each in phase 3)
 constexpr TileShape kF64Tiles[F64_NVAR] = {{32, 8}, {16, 16}, {64, 4}};
-constexpr int MX_NVAR = 2;  // 32 x 32 (256 threads), 32 x 16 (128 threads)
-constexpr TileShape kMxTiles[MX_NVAR] = {{32, 32}, {32, 16}};
+// Mixed lane: tile shape x halo-staging schedule of phase 1.  kStageLoads: each
+// thread loads its cells' raw inputs into registers and stores the derived cell
+// quantities; kStageAsync: asynchronous copies (cp.async) put the raw inputs of all
+// of a thread's cells into shared memory at once, then the thread derives the
+// quantities in place.
+constexpr int kStageLoads = 0, kStageAsync = 1;
+constexpr int MX_NVAR = 4;  // 32 x 32 (256 threads), 32 x 16 (128 threads); each with both schedules
+constexpr TileShape kMxTiles[MX_NVAR] = {{32, 32}, {32, 16}, {32, 32}, {32, 16}};
+constexpr int kMxStaging[MX_NVAR] = {kStageLoads, kStageLoads, kStageAsync, kStageAsync};
 
 // kernel launchers (return cudaGetLastError()); `var` indexes the tile tables
 cudaError_t launch_f64_stage(int var, const F64Stage *d_stages, const WorkItem *d_work, int nwork, int grid,

@@ -160,6 +160,17 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   return r;
 }
 
+// 4-byte asynchronous copy global -> shared (cp.async, through L1), and the wait
+// for every copy this thread has issued
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // 60 dx times the 6th-order centred derivative (spatial_operators_mod.F90:165,169)
 // of the values f[-3s .. 3s], the FMAs written out so that every build rounds the
 // same way
@@ -321,7 +332,8 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
 constexpr int kP1Unroll = CCS_MIXED_P1_UNROLL;
 
 // CENTRAL: the central-difference operators (no face phases); else WENO-Z.
-template <class T, bool CENTRAL, bool EDISS>
+// STG: the halo-staging schedule of phase 1 (kStageLoads or kStageAsync).
+template <class T, bool CENTRAL, bool EDISS, int STG>
 __global__ void __launch_bounds__(T::NT, CCS_MIXED_MIN_CTAS * 32 / T::TY)
 mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__restrict__ work, int nwork) {
   constexpr int TX = T::TX, TY = T::TY, NT = T::NT, RX = T::RX, RY = T::RY;
@@ -353,7 +365,60 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     const int i0 = 1 + wi.tx * TX, j0 = 1 + wi.ty * TY;
 
     // ---- phase 1: cell quantities on the halo'd tile ------------------------
-    {
+    if constexpr (STG == kStageAsync) {
+      // the raw inputs of every cell this thread stages go straight into the tile
+      // arrays by asynchronous copies, all in flight at once and none through
+      // registers; after its own copies land, the thread turns each of its cells
+      // into the cell quantities in place
+      const float phibar = st.phibar, ha2 = 0.5f * st.a2;
+      const float *__restrict__ ihp = st.in.hp, *__restrict__ iu = st.in.u, *__restrict__ iv = st.in.v;
+      const MeshMixed m = st.m;
+      for (int r = tid; r < RX * RY; r += NT) {
+        const int li = r % RX, lj = r / RX;
+        const int i = i0 - 3 + li, j = j0 - 3 + lj;
+        const int64_t c = L.idx(i, j, p), cs = L.idx(i, j, 0);
+        const int a = lj * SP + li;
+        if (i <= N + 3 && j <= N + 3 && !corner(i, j, N) && ccs_inb(c, L.field, 101) &&
+            ccs_inb(cs, L.panel, 102) && ccs_inb(a, T::RN, 103)) {
+          const float *g = reinterpret_cast<const float *>(m.ig + cs);
+          cp_async4(&S.F[a], ihp + c);
+          cp_async4(&S.u[a], iu + c);
+          cp_async4(&S.v[a], iv + c);
+          cp_async4(&S.s[a], m.s + cs);
+          cp_async4(&S.G[a], g);
+          cp_async4(&S.E[a], g + 1);
+          cp_async4(&S.uC[a], g + 2);
+          cp_async4(&S.vC[a], g + 3);
+          cp_async4(&S.hs[a], m.phis + c);
+        }
+      }
+      cp_async_wait_all();
+      for (int r = tid; r < RX * RY; r += NT) {
+        const int li = r % RX, lj = r / RX;
+        const int i = i0 - 3 + li, j = j0 - 3 + lj;
+        const int a = lj * SP + li;
+        if (!ccs_inb(a, T::RN, 103)) continue;
+        float F = 0.f, G = 0.f, E = 0.f, hs = 0.f, sc = 1.f, uC = 0.f, vC = 0.f, u = 0.f, v = 0.f;
+        if (i <= N + 3 && j <= N + 3 && !corner(i, j, N)) {
+          const float hp = S.F[a];
+          u = S.u[a];
+          v = S.v[a];
+          sc = S.s[a];
+          const float4 g = make_float4(S.G[a], S.E[a], S.uC[a], S.vC[a]);
+          uC = fmaf(g.x, u, g.y * v);
+          vC = fmaf(g.z, u, g.w * v);
+          const float mass = (phibar + hp) * sc;  // phiG / a^2
+          F = mass * uC;
+          G = mass * vC;
+          hs = S.hs[a] + hp;
+          E = fmaf(ha2, fmaf(u, uC, v * vC), hs);  // E - phibar
+        }
+        S.F[a] = F; S.G[a] = G; S.E[a] = E; S.hs[a] = hs; S.s[a] = sc;
+        S.uC[a] = uC; S.vC[a] = vC; S.u[a] = u; S.v[a] = v;
+      }
+    } else {
+      // each thread loads its cells' raw inputs into registers (coalesced rows of the
+      // halo'd tile) and stores the derived cell quantities
       const float phibar = st.phibar, ha2 = 0.5f * st.a2;
       const float *__restrict__ ihp = st.in.hp, *__restrict__ iu = st.in.u, *__restrict__ iv = st.in.v;
       const MeshMixed m = st.m;
@@ -695,48 +760,62 @@ using MxT0 = MxTile<32>;
 using MxT1 = MxTile<16>;
 static_assert(MxT0::TX == kMxTiles[0].tx && MxT0::TY == kMxTiles[0].ty, "tile table");
 static_assert(MxT1::TX == kMxTiles[1].tx && MxT1::TY == kMxTiles[1].ty, "tile table");
+static_assert(MxT0::TX == kMxTiles[2].tx && MxT0::TY == kMxTiles[2].ty, "tile table");
+static_assert(MxT1::TX == kMxTiles[3].tx && MxT1::TY == kMxTiles[3].ty, "tile table");
+static_assert(kMxStaging[0] == kStageLoads && kMxStaging[1] == kStageLoads && kMxStaging[2] == kStageAsync &&
+                  kMxStaging[3] == kStageAsync,
+              "staging table");
 
-template <class T>
+template <class T, int STG>
 int mx_grid_for(int device) {  // the WENO instance bounds the occupancy of all
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   constexpr int smem = (int)sizeof(SmemMx<T>);
-  cudaFuncSetAttribute(mixed_stage_kernel<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel<T, false, false>, T::NT, smem);
+  cudaFuncSetAttribute(mixed_stage_kernel<T, false, false, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mixed_stage_kernel<T, false, false, STG>, T::NT, smem);
   if (per < 1) per = 1;
   return sms * per;
 }
 
-template <class T, bool CENTRAL, bool EDISS>
+template <class T, bool CENTRAL, bool EDISS, int STG>
 cudaError_t mx_launch(const MixedStage *d_stages, const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
   constexpr int smem = (int)sizeof(SmemMx<T>);
   static std::atomic<uint64_t> attr_done{0};
-  const cudaError_t e = smem_attr_once((const void *)mixed_stage_kernel<T, CENTRAL, EDISS>, smem, attr_done);
+  const cudaError_t e = smem_attr_once((const void *)mixed_stage_kernel<T, CENTRAL, EDISS, STG>, smem, attr_done);
   if (e != cudaSuccess) return e;
   if (grid > nwork) grid = nwork;
   if (grid < 1) return cudaSuccess;
-  mixed_stage_kernel<T, CENTRAL, EDISS><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
+  mixed_stage_kernel<T, CENTRAL, EDISS, STG><<<grid, T::NT, smem, s>>>(d_stages, d_work, nwork);
   return cudaGetLastError();
 }
 
-template <class T>
+template <class T, int STG>
 cudaError_t mx_launch_any(bool central, bool ediss, const MixedStage *d_stages, const WorkItem *d_work, int nwork,
                           int grid, cudaStream_t s) {
-  if (central) return mx_launch<T, true, false>(d_stages, d_work, nwork, grid, s);  // no faces: no E term
-  if (ediss) return mx_launch<T, false, true>(d_stages, d_work, nwork, grid, s);
-  return mx_launch<T, false, false>(d_stages, d_work, nwork, grid, s);
+  if (central) return mx_launch<T, true, false, STG>(d_stages, d_work, nwork, grid, s);  // no faces: no E term
+  if (ediss) return mx_launch<T, false, true, STG>(d_stages, d_work, nwork, grid, s);
+  return mx_launch<T, false, false, STG>(d_stages, d_work, nwork, grid, s);
 }
 
 }  // namespace
 
 int mixed_max_grid(int var, int device) {
-  return var == 1 ? mx_grid_for<MxT1>(device) : mx_grid_for<MxT0>(device);
+  switch (var) {
+    case 1: return mx_grid_for<MxT1, kStageLoads>(device);
+    case 2: return mx_grid_for<MxT0, kStageAsync>(device);
+    case 3: return mx_grid_for<MxT1, kStageAsync>(device);
+    default: return mx_grid_for<MxT0, kStageLoads>(device);
+  }
 }
 
 cudaError_t launch_mixed_stage(int var, bool central, bool ediss, const MixedStage *d_stages,
                                const WorkItem *d_work, int nwork, int grid, cudaStream_t s) {
-  return var == 1 ? mx_launch_any<MxT1>(central, ediss, d_stages, d_work, nwork, grid, s)
-                  : mx_launch_any<MxT0>(central, ediss, d_stages, d_work, nwork, grid, s);
+  switch (var) {
+    case 1: return mx_launch_any<MxT1, kStageLoads>(central, ediss, d_stages, d_work, nwork, grid, s);
+    case 2: return mx_launch_any<MxT0, kStageAsync>(central, ediss, d_stages, d_work, nwork, grid, s);
+    case 3: return mx_launch_any<MxT1, kStageAsync>(central, ediss, d_stages, d_work, nwork, grid, s);
+    default: return mx_launch_any<MxT0, kStageLoads>(central, ediss, d_stages, d_work, nwork, grid, s);
+  }
 }
 
 static int ew_grid(const Layout &L) {

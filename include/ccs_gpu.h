@@ -173,10 +173,13 @@ int ccs_get_state_async(ccs_handle *h, ccs_state_view *s);
 int ccs_set_operator(ccs_handle *h, int op);
 
 /* ---- kernel variants and the autotuner (no counterpart in the reference) ----
- * Each lane's stage kernel comes in tile-shape variants (cells per work item):
- * FP64 lane 0: 32x8, 1: 16x16, 2: 64x4; mixed lane 0: 32x32, 1: 32x16.  Every
- * variant computes the same per-cell arithmetic, so results do not depend on the
- * choice.  ccs_autotune times the handle's RK stages before the last one (they write
+ * Each lane's stage kernel comes in variants: FP64 lane tile shapes (cells per
+ * work item) 0: 32x8, 1: 16x16, 2: 64x4; mixed lane tile shape and halo-staging
+ * schedule 0: 32x32 and 1: 32x16 with per-thread loads (each thread loads its
+ * cells' raw inputs into registers and stores the derived quantities), 2: 32x32
+ * and 3: 32x16 with asynchronous copies (the raw inputs of all of a thread's cells
+ * go into shared memory at once, then are derived in place).  Every variant
+ * computes the same per-cell arithmetic, so results do not depend on the choice.  ccs_autotune times the handle's RK stages before the last one (they write
  * only stage scratch, so the state is unchanged), `reps` rounds with each variant
  * after one warm-up launch, and keeps the fastest mean stage time; the choice is cached per (device, lane, N,
  * halo) for the process, and later calls with force = 0 reuse it without timing.

@@ -61,7 +61,7 @@ def main():
                 g.get_state()
                 hits(f"fp64 C{N} h{halo} tile {var} {scheme} ediss {ediss}")
                 healthy(g, f"fp64 C{N} h{halo} tile {var} {scheme} ediss {ediss}")
-        for var in (0, 1):
+        for var in range(len(L.MIXED_VARIANTS)):
             for scheme, ediss, op in (("RK4", 0, L.CCS_OP_WENO), ("RK3_TVD", 1, L.CCS_OP_WENO),
                                       ("RK4", 0, L.CCS_OP_CENTRAL4)):
                 g = M.Stepper(mesh, dt, precision="mixed", scheme=scheme, e_dissipation=ediss, operator=op, **kw)

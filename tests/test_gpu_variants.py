@@ -32,18 +32,20 @@ def test_fp64_variants_bitwise_against_oracle(var, N):
 
 @pytest.mark.parametrize("N", [40, 64])
 def test_mixed_variants_agree_bitwise(N):
+    """Both tile shapes with both halo-staging schedules give the same bits."""
     mesh, s, dt = seeded_case(N, 3, seed=6, oro=True)
     out = []
-    for var in (0, 1):
+    for var, (tx, ty, _) in enumerate(L.MIXED_VARIANTS):
         g = M.Stepper(mesh, dt, precision="mixed", phi_mean=8000.0 * mesh.gravity)
         g.set_variant(var)
-        assert g.variant == ((0, 32, 32), (1, 32, 16))[var]
+        assert g.variant == (var, tx, ty)
         g.set_state(s)
         g.step(5)
         out.append(g.get_state())
     m = valid_mask(mesh)
-    for k in CHECK_FIELDS:
-        assert bitwise_equal(out[0][k], out[1][k], m), k
+    for var in range(1, len(out)):
+        for k in CHECK_FIELDS:
+            assert bitwise_equal(out[0][k], out[var][k], m), (var, k)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -55,7 +57,7 @@ def test_autotune_keeps_state_and_caches(precision):
     g.step(1)
     before = g.get_state()
     var, times = g.autotune(reps=3, force=True)
-    nvar = 3 if precision == "fp64" else 2
+    nvar = 3 if precision == "fp64" else len(L.MIXED_VARIANTS)
     assert 0 <= var < nvar and all(t > 0 for t in times[:nvar]) and times[var] == min(times[:nvar])
     assert g.variant[0] == var
     after = g.get_state()
@@ -91,7 +93,7 @@ def test_batch_runs_one_launch_per_lane_whatever_the_members_variants():
         x.set_state(s)
         members.append(x)
         lanes.append("fp64")
-    for var in (1, 0):
+    for var in (1, 0, 3, 2):
         y = M.Stepper(mesh, dt, precision="mixed", **kw)
         y.set_variant(var)
         y.set_state(s)
@@ -100,7 +102,7 @@ def test_batch_runs_one_launch_per_lane_whatever_the_members_variants():
     b = M.Batch(members)
     launches, groups = b.info()
     assert launches == 2
-    assert sorted((lane, n) for lane, _, n in groups) == [(L.CCS_FP64, 3), (L.CCS_MIXED, 2)]
+    assert sorted((lane, n) for lane, _, n in groups) == [(L.CCS_FP64, 3), (L.CCS_MIXED, 4)]
     b.step(1)
     b.autotune(reps=2)
     assert b.info()[0] == 2
