@@ -235,7 +235,7 @@ class Stepper:
             self.set_operator(operator)
 
     def set_operator(self, op: int):
-        """The spatial operator (CCS_OP_WENO or CCS_OP_CENTRAL2/4/6), FP64 lane."""
+        """The spatial operator (CCS_OP_WENO or CCS_OP_CENTRAL2/4/6), either lane."""
         L.check(L.lib().ccs_set_operator(self.handle, int(op)), "ccs_set_operator", self.handle)
 
     def autotune(self, reps: int = 5, force: bool = False):
