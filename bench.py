@@ -473,6 +473,19 @@ def run_uneven(torch, steps: int, warmup: int) -> dict:
     launches, info = batch.info()
     tiles = {"fp64" if lane == 0 else "mixed": var for lane, var, _ in info}
     names = {k: variant_name(k, v) for k, v in tiles.items()}
+    # the same mixed members batched without the FP64 ones: the FP64 lane's stages
+    # (FP64-pipe bound) pace the mixed batch above
+    batch.close()
+    mixed_only = M.Batch([m for m in members if m.precision == "mixed"])
+    mixed_only.autotune(reps=3)
+    mixed_only.step(max(warmup, 3))
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    t32 = slowest_rank_seconds(_batch_time(mixed_only, torch, steps))
+    alg32 = ALG_BYTES_MIXED * cells32 * steps / t32 / 1e9
+    n32, info32 = mixed_only.info()
+    mixed_only.close()
     return {
         "cell_steps_per_s": ws * cells * steps / t, "steps": steps, "warmup": max(warmup, 3),
         "ms_per_step": 1e3 * t / steps, "hbm_frac": ws * alg / (_peaks()[0] * ws), "alg_GBs": ws * alg,
@@ -481,6 +494,11 @@ def run_uneven(torch, steps: int, warmup: int) -> dict:
         "instances": len(members),
         "how": "29 instances with per-instance CFL dt, one FP64 member per resolution below C384; one graph per "
                "step, each lane's stages on its own stream; CUDA events on the batch stream",
+        "mixed_members_alone": {
+            "cell_steps_per_s": ws * cells32 * steps / t32, "ms_per_step": 1e3 * t32 / steps,
+            "hbm_frac": alg32 / _peaks()[0], "alg_GBs": ws * alg32, "launches_per_stage": n32,
+            "variant": variant_name("mixed", info32[0][1]) if info32 else None,
+            "how": "the 26 mixed instances in a batch of their own, same timing"},
     }
 
 

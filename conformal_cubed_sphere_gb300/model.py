@@ -217,6 +217,7 @@ class Stepper:
                  share_with: "Stepper | None" = None, operator: int = L.CCS_OP_WENO):
         self.mesh = mesh
         self.dt = float(dt)
+        self.precision = "fp64" if precision == "fp64" else "mixed"
         cfg = L.Config(N=mesh.N, halo=mesh.halo, scheme=L.CCS_RK4 if scheme == "RK4" else L.CCS_RK3_TVD,
                        precision=L.CCS_FP64 if precision == "fp64" else L.CCS_MIXED,
                        e_dissipation=e_dissipation, device=device, dx=mesh.dx, dy=mesh.dy, dt=self.dt,
