@@ -799,12 +799,13 @@ static int mixed_mesh_setup(ccs_handle *h, DeviceMesh *dm, const ccs_mesh_view *
         fs[d] = (float)(mv->f[r] * sg / a2);
       }
   // face wave-speed metric (spatial_operators_mod.F90:113-114, 138-139), x-faces i in
-  // [0, N] of rows j in [1, N] and y-faces j in [0, N] of columns i in [1, N]
+  // [0, N] of rows j in [1, N] (stored transposed) and y-faces j in [0, N] of columns
+  // i in [1, N]
   for (int j = 0; j <= N; j++)
     for (int i = 0; i <= N; i++) {
       const size_t r = (size_t)(i + hh - 1) + (size_t)nh * (size_t)(j + hh - 1);
       const int64_t d = L.idx(i, j, 0);
-      if (j >= 1) sh_lamx[d] = (float)(0.5 * (mv->matrixIG[4 * (r + 1)] + mv->matrixIG[4 * r]));
+      if (j >= 1) sh_lamx[L.idx(j, i, 0)] = (float)(0.5 * (mv->matrixIG[4 * (r + 1)] + mv->matrixIG[4 * r]));
       if (i >= 1) sh_lamy[d] = (float)(0.5 * (mv->matrixIG[4 * (r + nh) + 3] + mv->matrixIG[4 * r + 3]));
     }
   CCS_TRY(h, cudaMemcpyAsync(dm->buf32, hb.data(), nfloat * sizeof(float), cudaMemcpyHostToDevice, h->stream));

@@ -81,8 +81,10 @@ struct MeshMixed {
   const float *s, *inv_s;
   const float4 *ig;  // (IG11, IG12, IG21, IG22) * a^2 of each cell of the panel
 
-  // static wave-speed metric of the faces: lamx at the x-face right of cell (i, j)
-  // is (IG11(i,j) + IG11(i+1,j)) / 2, lamy likewise for the y-face above it
+  // static wave-speed metric of the faces: the x-face right of cell (i, j) has
+  // (IG11(i,j) + IG11(i+1,j)) / 2, stored transposed at lamx[idx(j, i, 0)]; the
+  // y-face above cell (i, j) has (IG22(i,j) + IG22(i,j+1)) / 2 at lamy[idx(i, j, 0)].
+  // Both keep the face index in the row position, so a line sweep steps by the pitch.
   const float *lamx, *lamy;
   const float *phis, *fs;
   const double *xf;

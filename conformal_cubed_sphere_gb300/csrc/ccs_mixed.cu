@@ -36,6 +36,24 @@ struct MxTile {
 };
 constexpr int SP = 39;  // the smem row pitch, the same for every tile height
 
+// a / b as a times the approximate reciprocal of b (rcp.approx.ftz.f32: one MUFU
+// instruction, a few ulp).  Every denominator here is eps + beta >= eps (at least
+// 1e-30 after the rescaling) or a sum of WENO weights >= 1, far from the range where
+// the reciprocal would flush; the result equals __fdividef's on these operands
+// without that intrinsic's range handling.
+__device__ __forceinline__ float qdiv(float a, float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return a * r;
+}
+
+// min(a, b, c) in one three-input min.f32 instruction
+__device__ __forceinline__ float min3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Difference-form WENO-Z (spatial_operators_mod.F90:282-361) of one cell for both
 // directions.  d0..d3 = Q(c-1)-Q(c-2), Q(c)-Q(c-1), Q(c+1)-Q(c), Q(c+2)-Q(c+1).
 // Returns Dp = Rec+(c) - Q(c) (face c+1/2) and Dm = Rec-(c) - Q(c) (face c-1/2).
@@ -51,10 +69,10 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
   const float b2 = fmaf(k133 * A2, A2, B2 * B2);
   const float b3 = fmaf(k133 * A3, A3, B3 * B3);
   const float t40 = fabsf(b1 - b2), t41 = fabsf(b2 - b3), t5 = fabsf(b3 - b1);
-  const float mn = fminf(b1, fminf(b2, b3));
-  const float r1 = __fdividef(t5, eps + b1);
-  const float r2 = __fdividef(t5, eps + b2);
-  const float r3 = __fdividef(t5, eps + b3);
+  const float mn = min3(b1, b2, b3);
+  const float r1 = qdiv(t5, eps + b1);
+  const float r2 = qdiv(t5, eps + b2);
+  const float r3 = qdiv(t5, eps + b3);
   // candidate corrections S_k - Q(c)
   const float p1 = fmaf(5.f / 6.f, d1, -(1.f / 3.f) * d0);
   const float p2 = fmaf(1.f / 6.f, d1, (1.f / 3.f) * d2);
@@ -72,14 +90,14 @@ __device__ __forceinline__ void weno_d(float d0, float d1, float d2, float d3, f
   {  // "+" weights
     const float a1 = fmaf(0.1f, r1, 0.1f), a2 = fmaf(0.6f, r2, 0.6f), a3 = fmaf(0.3f, r3, 0.3f);
     const float num = fmaf(a1, p1, fmaf(a2, p2, a3 * p3));
-    float val = __fdividef(num, a1 + a2 + a3);
+    float val = qdiv(num, a1 + a2 + a3);
     val = (hi40 && lt41) ? sb : val;
     Dp = (lo40 && hi41) ? sa : val;
   }
   {  // "-" weights: beta' = (b3, b2, b1), tau40' = t41, tau41' = t40
     const float a1 = fmaf(0.1f, r3, 0.1f), a2 = fmaf(0.6f, r2, 0.6f), a3 = fmaf(0.3f, r1, 0.3f);
     const float num = fmaf(a1, m1, fmaf(a2, m2, a3 * m3));
-    float val = __fdividef(num, a1 + a2 + a3);
+    float val = qdiv(num, a1 + a2 + a3);
     val = (hi41 && lt40) ? tb : val;
     Dm = (lo41 && hi40) ? ta : val;
   }
@@ -120,9 +138,9 @@ __device__ __forceinline__ void weno_d2(float2 d0, float2 d1, float2 d2, float2 
 #pragma unroll
   for (int q = 0; q < 2; q++) {
     const float t40 = fabsf(q ? D12.y : D12.x), t41 = fabsf(q ? D23.y : D23.x), t5 = fabsf(q ? D31.y : D31.x);
-    const float mn = fminf(q ? b1.y : b1.x, fminf(q ? b2.y : b2.x, q ? b3.y : b3.x));
-    const float x1 = __fdividef(t5, q ? e1.y : e1.x), x2 = __fdividef(t5, q ? e2.y : e2.x),
-                x3 = __fdividef(t5, q ? e3.y : e3.x);
+    const float mn = min3(q ? b1.y : b1.x, q ? b2.y : b2.x, q ? b3.y : b3.x);
+    const float x1 = qdiv(t5, q ? e1.y : e1.x), x2 = qdiv(t5, q ? e2.y : e2.x),
+                x3 = qdiv(t5, q ? e3.y : e3.x);
     if (q) { r1.y = x1; r2.y = x2; r3.y = x3; } else { r1.x = x1; r2.x = x2; r3.x = x3; }
     lo40[q] = t40 <= mn; lo41[q] = t41 <= mn; hi40[q] = !lo40[q]; hi41[q] = !lo41[q];
     lt40[q] = t40 < mn; lt41[q] = t41 < mn;
@@ -132,7 +150,7 @@ __device__ __forceinline__ void weno_d2(float2 d0, float2 d1, float2 d2, float2 
                  a3 = __ffma2_rn(k2(0.3f), r3, k2(0.3f));
     const float2 num = __ffma2_rn(a1, p1, __ffma2_rn(a2, p2, __fmul2_rn(a3, p3)));
     const float2 den = __fadd2_rn(__fadd2_rn(a1, a2), a3);
-    float vx = __fdividef(num.x, den.x), vy = __fdividef(num.y, den.y);
+    float vx = qdiv(num.x, den.x), vy = qdiv(num.y, den.y);
     vx = (hi40[0] && lt41[0]) ? sb.x : vx;
     vy = (hi40[1] && lt41[1]) ? sb.y : vy;
     Dp.x = (lo40[0] && hi41[0]) ? sa.x : vx;
@@ -143,7 +161,7 @@ __device__ __forceinline__ void weno_d2(float2 d0, float2 d1, float2 d2, float2 
                  a3 = __ffma2_rn(k2(0.3f), r1, k2(0.3f));
     const float2 num = __ffma2_rn(a1, m1, __ffma2_rn(a2, m2, __fmul2_rn(a3, m3)));
     const float2 den = __fadd2_rn(__fadd2_rn(a1, a2), a3);
-    float vx = __fdividef(num.x, den.x), vy = __fdividef(num.y, den.y);
+    float vx = qdiv(num.x, den.x), vy = qdiv(num.y, den.y);
     vx = (hi41[0] && lt40[0]) ? tb.x : vx;
     vy = (hi41[1] && lt40[1]) ? tb.y : vy;
     Dm.x = (lo41[0] && hi40[0]) ? ta.x : vx;
@@ -250,8 +268,10 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
   // face wave-speed metric, fetched one face ahead of its use by walking a pointer
   // along the line; faces of a partial tile beyond N are read (and not used) from
   // the 32 padding rows the metric arrays carry after each panel block
-  const float *lp = lam + (XDIR ? L.idx(startg + f0, lineg, 0) : L.idx(lineg, startg + f0, 0));
-  const int lstride = XDIR ? 1 : L.pitch;
+  // (both face metrics are stored with the face index in the row position, so the
+  // threads of a warp, one line each, read consecutive addresses at every step)
+  const float *lp = lam + L.idx(lineg, startg + f0, 0);
+  const int lstride = L.pitch;
   const long long lam_n = L.panel + (long long)kLamPadRows * L.pitch;  // face-metric block + padding
   float lam_next = ccs_inb(lp - lam, lam_n, 115) ? __ldg(lp) : 0.f;
   for (int k = 0; k <= NFACE; k++) {
@@ -325,9 +345,10 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
 #ifndef CCS_MIXED_MIN_CTAS
 #define CCS_MIXED_MIN_CTAS 3
 #endif
-// halo'd-tile cells each thread loads per round in phase 1 (loads in flight)
+// halo'd-tile cells each thread loads per round in phase 1 (loads in flight); one
+// cell per round measured fastest with three CTAs per SM
 #ifndef CCS_MIXED_P1_UNROLL
-#define CCS_MIXED_P1_UNROLL 2
+#define CCS_MIXED_P1_UNROLL 1
 #endif
 constexpr int kP1Unroll = CCS_MIXED_P1_UNROLL;
 
