@@ -341,6 +341,150 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
   }
 }
 
+// Phase 3 of a tile for stage kind KIND: the early global loads, the barrier after
+// the line phase, the tendencies and the stage update.
+template <int KIND, class T, bool CENTRAL>
+__device__ __forceinline__ void tile_update(SmemMx<T> &S, const Layout &L, int p, int i0, int j0, int lane,
+                                            int warp) {
+  constexpr int NT = T::NT;
+  const int N = L.N;
+  const MixedStage &st = S.st;
+  // Global operands of phase 3 for this thread's four cells, loaded before the
+  // barrier so their latency overlaps the wait for the slowest line segment:
+  // f s, 1/s, Y0, the accumulator (or the stage input's hp for RK3) and the
+  // compensation terms, as the stage kind needs them.
+  constexpr int kind = KIND;
+  constexpr bool need_acc = kind == K_RK4_2 || kind == K_RK4_4;
+  constexpr bool need_in = kind == K_RK3_2 || kind == K_RK3_3;
+  constexpr bool need_lo = kind == K_RK4_4 || kind == K_RK3_3;
+  float q_fs[4], q_is[4], q_y0[4][3], q_a[4][3], q_lo[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int i = i0 + lane, j = j0 + warp + (NT / 32) * k;
+    q_fs[k] = q_is[k] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 3; q++) q_y0[k][q] = q_a[k][q] = q_lo[k][q] = 0.f;
+    if (i > N || j > N) continue;
+    const int64_t c = L.idx(i, j, p);
+    if (!ccs_inb(c, L.field, 121) || !ccs_inb(L.idx(i, j, 0), L.panel, 122)) continue;
+    q_fs[k] = __ldg(st.m.fs + c);
+    q_is[k] = __ldg(st.m.inv_s + L.idx(i, j, 0));
+    if constexpr (kind == K_TEND) continue;
+    q_y0[k][0] = st.y0hp[c]; q_y0[k][1] = st.y0u[c]; q_y0[k][2] = st.y0v[c];
+    if (need_acc) { q_a[k][0] = st.acchp[c]; q_a[k][1] = st.accu[c]; q_a[k][2] = st.accv[c]; }
+    if (need_in) q_a[k][0] = st.in.hp[c];
+    if (need_lo) { q_lo[k][0] = st.lohp[c]; q_lo[k][1] = st.lou[c]; q_lo[k][2] = st.lov[c]; }
+  }
+  __syncthreads();
+
+  // ---- phase 3: tendencies, stage update ---------------------------------------
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int li = lane, lj = warp + (NT / 32) * k;
+    const int i = i0 + li, j = j0 + lj;
+    if (i > N || j > N) continue;
+    const int r = (lj + 3) * SP + li + 3;
+    if (!ccs_inb(r - 3 * SP, T::RN, 131) || !ccs_inb(r + 3 * SP, T::RN, 132) ||
+        !ccs_inb((long long)lj * T::NFL + li + 1, (long long)T::TY * T::NFL, 133) ||
+        !ccs_inb((long long)(lj + 1) * T::TX + li, (long long)(T::TY + 1) * T::TX, 134) ||
+        !ccs_inb(L.idx(i, j, p), L.field, 135))
+      continue;
+    float divx, dEdx, divy, dEdy, dvdx, dudy;
+    if (!CENTRAL) {
+      divx = (S.gx[0][lj][li + 1] - S.gx[0][lj][li] + (S.F[r] - S.F[r - 1])) * st.rdx;
+      dEdx = (S.gx[1][lj][li + 1] - S.gx[1][lj][li] + (S.E[r] - S.E[r - 1])) * st.rdx;
+      divy = (S.gy[0][lj + 1][li] - S.gy[0][lj][li] + (S.G[r] - S.G[r - SP])) * st.rdy;
+      dEdy = (S.gy[1][lj + 1][li] - S.gy[1][lj][li] + (S.E[r] - S.E[r - SP])) * st.rdy;
+      dvdx = diff6(S.v + r, 1) * st.rdx60;
+      dudy = diff6(S.u + r, SP) * st.rdy60;
+    } else {  // spatial_operators_mod_{2nd,4th,6th}.F90: centred differences of the cell values
+      const int op = st.op;
+      divx = central(op, S.F + r, 1) * st.rdxc;
+      dEdx = central(op, S.E + r, 1) * st.rdxc;
+      dvdx = central(op, S.v + r, 1) * st.rdxc;
+      divy = central(op, S.G + r, SP) * st.rdyc;
+      dEdy = central(op, S.E + r, SP) * st.rdyc;
+      dudy = central(op, S.u + r, SP) * st.rdyc;
+    }
+    const int64_t c = L.idx(i, j, p);
+    const float vort = dvdx - dudy + q_fs[k];
+    const float tp = -(divx + divy) * q_is[k];
+    const float tu = fmaf(vort, S.vC[r], -dEdx * st.inv_a2);
+    const float tv = fmaf(-vort, S.uC[r], -dEdy * st.inv_a2);
+    if (kind == K_TEND) {
+      st.thp[c] = tp;
+      st.tu[c] = tu;
+      st.tv[c] = tv;
+      continue;
+    }
+    const float y0p = q_y0[k][0], y0u = q_y0[k][1], y0v = q_y0[k][2];
+    float ip, iu, iv;  // increments to Y0 (Y = Y0 + c1 k fused where the stage is linear)
+    bool fin = false, lin = false;
+    switch (kind) {
+      case K_RK4_1:
+        st.acchp[c] = tp; st.accu[c] = tu; st.accv[c] = tv;
+        ip = tp; iu = tu; iv = tv;
+        lin = true;
+        break;
+      case K_RK4_2:
+        st.acchp[c] = fmaf(2.f, tp, q_a[k][0]);
+        st.accu[c] = fmaf(2.f, tu, q_a[k][1]);
+        st.accv[c] = fmaf(2.f, tv, q_a[k][2]);
+        ip = tp; iu = tu; iv = tv;
+        lin = true;
+        break;
+      case K_RK4_4: {
+        const float k6 = st.c1 * (1.f / 6.f);
+        ip = k6 * (q_a[k][0] + tp); iu = k6 * (q_a[k][1] + tu); iv = k6 * (q_a[k][2] + tv);
+        fin = true;
+        break;
+      }
+      case K_RK3_1:
+        ip = tp; iu = tu; iv = tv;
+        lin = true;
+        break;
+      case K_RK3_2:
+        ip = fmaf(0.25f, q_a[k][0] - y0p, st.c1 * tp);
+        iu = fmaf(0.25f, S.u[r] - y0u, st.c1 * tu);
+        iv = fmaf(0.25f, S.v[r] - y0v, st.c1 * tv);
+        break;
+      default:  // K_RK3_3
+        ip = fmaf(2.f / 3.f, q_a[k][0] - y0p, st.c1 * tp);
+        iu = fmaf(2.f / 3.f, S.u[r] - y0u, st.c1 * tu);
+        iv = fmaf(2.f / 3.f, S.v[r] - y0v, st.c1 * tv);
+        fin = true;
+        break;
+    }
+    float np, nu, nv;
+    if (fin) {
+      // compensated update of the step-to-step state (TwoSum)
+      float lo[3] = {q_lo[k][0], q_lo[k][1], q_lo[k][2]};
+      const float hi[3] = {y0p, y0u, y0v};
+      const float inc[3] = {ip, iu, iv};
+      float out[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const float y = inc[q] + lo[q];
+        const float tt = hi[q] + y;
+        const float bp = tt - hi[q];
+        lo[q] = (hi[q] - (tt - bp)) + (y - bp);
+        out[q] = tt;
+      }
+      np = out[0]; nu = out[1]; nv = out[2];
+      st.lohp[c] = lo[0]; st.lou[c] = lo[1]; st.lov[c] = lo[2];
+    } else if (lin) {
+      np = fmaf(st.c1, ip, y0p); nu = fmaf(st.c1, iu, y0u); nv = fmaf(st.c1, iv, y0v);
+    } else {
+      np = y0p + ip; nu = y0u + iu; nv = y0v + iv;
+    }
+    st.out.hp[c] = np;
+    st.out.u[c] = nu;
+    st.out.v[c] = nv;
+  }
+  __syncthreads();
+
+}
+
 // resident CTAs per SM the register allocation targets (3: 80 registers)
 #ifndef CCS_MIXED_MIN_CTAS
 #define CCS_MIXED_MIN_CTAS 3
@@ -485,139 +629,19 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         if (i0 + line <= N) tile_line<false, EDISS>(S, S.G, S.vC, st.m.lamy, L, line, f0, nface, j0 - 1, i0 + line);
       }
     }
-    // Global operands of phase 3 for this thread's four cells, loaded before the
-    // barrier so their latency overlaps the wait for the slowest line segment:
-    // f s, 1/s, Y0, the accumulator (or the stage input's hp for RK3) and the
-    // compensation terms, as the stage kind needs them (uniform over the CTA).
-    const int kind = st.kind;
-    const bool need_acc = kind == K_RK4_2 || kind == K_RK4_4;
-    const bool need_in = kind == K_RK3_2 || kind == K_RK3_3;
-    const bool need_lo = kind == K_RK4_4 || kind == K_RK3_3;
-    float q_fs[4], q_is[4], q_y0[4][3], q_a[4][3], q_lo[4][3];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int i = i0 + lane, j = j0 + warp + (NT / 32) * k;
-      q_fs[k] = q_is[k] = 0.f;
-#pragma unroll
-      for (int q = 0; q < 3; q++) q_y0[k][q] = q_a[k][q] = q_lo[k][q] = 0.f;
-      if (i > N || j > N) continue;
-      const int64_t c = L.idx(i, j, p);
-      if (!ccs_inb(c, L.field, 121) || !ccs_inb(L.idx(i, j, 0), L.panel, 122)) continue;
-      q_fs[k] = __ldg(st.m.fs + c);
-      q_is[k] = __ldg(st.m.inv_s + L.idx(i, j, 0));
-      if (kind == K_TEND) continue;
-      q_y0[k][0] = st.y0hp[c]; q_y0[k][1] = st.y0u[c]; q_y0[k][2] = st.y0v[c];
-      if (need_acc) { q_a[k][0] = st.acchp[c]; q_a[k][1] = st.accu[c]; q_a[k][2] = st.accv[c]; }
-      if (need_in) q_a[k][0] = st.in.hp[c];
-      if (need_lo) { q_lo[k][0] = st.lohp[c]; q_lo[k][1] = st.lou[c]; q_lo[k][2] = st.lov[c]; }
+    // phase 3 as an instance per stage kind: the stage kind is the same for every
+    // work item of a launch (a batch groups its members by RK scheme and launches
+    // one stage at a time), so the stage update carries no runtime branches and
+    // loads only the operands its kind uses
+    switch (st.kind) {
+      case K_RK4_1: tile_update<K_RK4_1, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
+      case K_RK4_2: tile_update<K_RK4_2, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
+      case K_RK4_4: tile_update<K_RK4_4, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
+      case K_RK3_1: tile_update<K_RK3_1, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
+      case K_RK3_2: tile_update<K_RK3_2, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
+      case K_RK3_3: tile_update<K_RK3_3, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
+      default: tile_update<K_TEND, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
     }
-    __syncthreads();
-
-    // ---- phase 3: tendencies, stage update ---------------------------------------
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int li = lane, lj = warp + (NT / 32) * k;
-      const int i = i0 + li, j = j0 + lj;
-      if (i > N || j > N) continue;
-      const int r = (lj + 3) * SP + li + 3;
-      if (!ccs_inb(r - 3 * SP, T::RN, 131) || !ccs_inb(r + 3 * SP, T::RN, 132) ||
-          !ccs_inb((long long)lj * T::NFL + li + 1, (long long)T::TY * T::NFL, 133) ||
-          !ccs_inb((long long)(lj + 1) * T::TX + li, (long long)(T::TY + 1) * T::TX, 134) ||
-          !ccs_inb(L.idx(i, j, p), L.field, 135))
-        continue;
-      float divx, dEdx, divy, dEdy, dvdx, dudy;
-      if (!CENTRAL) {
-        divx = (S.gx[0][lj][li + 1] - S.gx[0][lj][li] + (S.F[r] - S.F[r - 1])) * st.rdx;
-        dEdx = (S.gx[1][lj][li + 1] - S.gx[1][lj][li] + (S.E[r] - S.E[r - 1])) * st.rdx;
-        divy = (S.gy[0][lj + 1][li] - S.gy[0][lj][li] + (S.G[r] - S.G[r - SP])) * st.rdy;
-        dEdy = (S.gy[1][lj + 1][li] - S.gy[1][lj][li] + (S.E[r] - S.E[r - SP])) * st.rdy;
-        dvdx = diff6(S.v + r, 1) * st.rdx60;
-        dudy = diff6(S.u + r, SP) * st.rdy60;
-      } else {  // spatial_operators_mod_{2nd,4th,6th}.F90: centred differences of the cell values
-        const int op = st.op;
-        divx = central(op, S.F + r, 1) * st.rdxc;
-        dEdx = central(op, S.E + r, 1) * st.rdxc;
-        dvdx = central(op, S.v + r, 1) * st.rdxc;
-        divy = central(op, S.G + r, SP) * st.rdyc;
-        dEdy = central(op, S.E + r, SP) * st.rdyc;
-        dudy = central(op, S.u + r, SP) * st.rdyc;
-      }
-      const int64_t c = L.idx(i, j, p);
-      const float vort = dvdx - dudy + q_fs[k];
-      const float tp = -(divx + divy) * q_is[k];
-      const float tu = fmaf(vort, S.vC[r], -dEdx * st.inv_a2);
-      const float tv = fmaf(-vort, S.uC[r], -dEdy * st.inv_a2);
-      if (kind == K_TEND) {
-        st.thp[c] = tp;
-        st.tu[c] = tu;
-        st.tv[c] = tv;
-        continue;
-      }
-      const float y0p = q_y0[k][0], y0u = q_y0[k][1], y0v = q_y0[k][2];
-      float ip, iu, iv;  // increments to Y0 (Y = Y0 + c1 k fused where the stage is linear)
-      bool fin = false, lin = false;
-      switch (kind) {
-        case K_RK4_1:
-          st.acchp[c] = tp; st.accu[c] = tu; st.accv[c] = tv;
-          ip = tp; iu = tu; iv = tv;
-          lin = true;
-          break;
-        case K_RK4_2:
-          st.acchp[c] = fmaf(2.f, tp, q_a[k][0]);
-          st.accu[c] = fmaf(2.f, tu, q_a[k][1]);
-          st.accv[c] = fmaf(2.f, tv, q_a[k][2]);
-          ip = tp; iu = tu; iv = tv;
-          lin = true;
-          break;
-        case K_RK4_4: {
-          const float k6 = st.c1 * (1.f / 6.f);
-          ip = k6 * (q_a[k][0] + tp); iu = k6 * (q_a[k][1] + tu); iv = k6 * (q_a[k][2] + tv);
-          fin = true;
-          break;
-        }
-        case K_RK3_1:
-          ip = tp; iu = tu; iv = tv;
-          lin = true;
-          break;
-        case K_RK3_2:
-          ip = fmaf(0.25f, q_a[k][0] - y0p, st.c1 * tp);
-          iu = fmaf(0.25f, S.u[r] - y0u, st.c1 * tu);
-          iv = fmaf(0.25f, S.v[r] - y0v, st.c1 * tv);
-          break;
-        default:  // K_RK3_3
-          ip = fmaf(2.f / 3.f, q_a[k][0] - y0p, st.c1 * tp);
-          iu = fmaf(2.f / 3.f, S.u[r] - y0u, st.c1 * tu);
-          iv = fmaf(2.f / 3.f, S.v[r] - y0v, st.c1 * tv);
-          fin = true;
-          break;
-      }
-      float np, nu, nv;
-      if (fin) {
-        // compensated update of the step-to-step state (TwoSum)
-        float lo[3] = {q_lo[k][0], q_lo[k][1], q_lo[k][2]};
-        const float hi[3] = {y0p, y0u, y0v};
-        const float inc[3] = {ip, iu, iv};
-        float out[3];
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          const float y = inc[q] + lo[q];
-          const float tt = hi[q] + y;
-          const float bp = tt - hi[q];
-          lo[q] = (hi[q] - (tt - bp)) + (y - bp);
-          out[q] = tt;
-        }
-        np = out[0]; nu = out[1]; nv = out[2];
-        st.lohp[c] = lo[0]; st.lou[c] = lo[1]; st.lov[c] = lo[2];
-      } else if (lin) {
-        np = fmaf(st.c1, ip, y0p); nu = fmaf(st.c1, iu, y0u); nv = fmaf(st.c1, iv, y0v);
-      } else {
-        np = y0p + ip; nu = y0u + iu; nv = y0v + iv;
-      }
-      st.out.hp[c] = np;
-      st.out.u[c] = nu;
-      st.out.v[c] = nv;
-    }
-    __syncthreads();
 
     // ---- phase 4: ghost push of the tile's edge strips ----------------------
     // hp copies; the covariant wind crosses the edge through the FP64 2x2
