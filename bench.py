@@ -594,9 +594,9 @@ def main():
     hbm, peak_kind = _peaks()
     bytes_per_launch = ALG_BYTES_MIXED / 4.0 * cells
     achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
-    prof_var = counters.get("mixed_variant", 0)
-    same_kernel = mesh.N == 384 and mixed.variant[0] == prof_var
-    traffic = counters.get("mixed_stage_C384") if same_kernel else None
+    # ncu counters of the variant the autotuner chose (taken at C384 for each mixed variant)
+    prof = counters.get("mixed_C384", {}).get(str(mixed.variant[0]), {}) if mesh.N == 384 else {}
+    traffic = prof.get("dram_bytes")
 
     # FP64 parity lane on the same state
     f64 = M.Stepper(mesh, dt, precision="fp64", device=local)
@@ -655,8 +655,7 @@ def main():
                      "kernel_ms_how": "timed step / 4 (events around each step's graph of four launches)",
                      "alg_bytes_per_launch": bytes_per_launch, "peak_source": peak_kind,
                      "counters_sha16": counters.get("sources_sha16"),
-                     "issue": issue_roofline(avg_ms, counters.get("mixed_stage_C384_warp_inst") if same_kernel
-                                             else None, sms, clocks)},
+                     "issue": issue_roofline(avg_ms, prof.get("warp_inst"), sms, clocks)},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "how": "ccs_set_state_async + ccs_step_async(1) + ccs_get_state_async per step, each state's "
                        "fields in one pinned host block (one copy per direction), one ccs_sync at the end",

@@ -214,7 +214,10 @@ __device__ __forceinline__ float central(int op, const float *f, int s) {
 
 template <class T>
 struct SmemMx {
-  MixedStage st;  // this work item's stage descriptor
+  // stage descriptors and work items of this tile and the next (double-buffered:
+  // the next tile's descriptor is copied while this one computes)
+  MixedStage stb[2];
+  WorkItem wib[2];
   // cell quantities on the halo'd tile, [row][col] with pitch SP
   float F[T::RN], G[T::RN], E[T::RN], hs[T::RN], s[T::RN], uC[T::RN], vC[T::RN], u[T::RN], v[T::RN];
   float gx[2][T::TY][T::NFL];     // x-face (flux, E) values minus the value of the cell left of the face
@@ -231,11 +234,10 @@ __device__ __forceinline__ bool corner(int i, int j, int N) { return (i < 1 || i
 // line (u at x-faces, v at y-faces: CCS_EDISS_RECONSTRUCT), reconstructed like the
 // other fields and paired with E in f32x2; its eps scales like the flux's (1e-2 / a^4).
 template <bool XDIR, bool EDISS, class T>
-__device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict__ Qflux,
+__device__ __forceinline__ void tile_line(SmemMx<T> &S, const MixedStage &st, const float *__restrict__ Qflux,
                                           const float *__restrict__ cvel, const float *__restrict__ lam,
                                           const Layout &L, int line, int f0,
                                           int NFACE, int startg, int lineg) {
-  const MixedStage &st = S.st;
   const float phibar = st.phibar, epsF = 4.f * st.eps_F, epsE = 4.f * st.eps_E, epsP = 4.f * st.eps_P;
   const float *__restrict__ Uw = XDIR ? S.u : S.v;  // the wind component along the line
   const int stp = XDIR ? 1 : SP;
@@ -344,11 +346,10 @@ __device__ __forceinline__ void tile_line(SmemMx<T> &S, const float *__restrict_
 // Phase 3 of a tile for stage kind KIND: the early global loads, the barrier after
 // the line phase, the tendencies and the stage update.
 template <int KIND, class T, bool CENTRAL>
-__device__ __forceinline__ void tile_update(SmemMx<T> &S, const Layout &L, int p, int i0, int j0, int lane,
-                                            int warp) {
+__device__ __forceinline__ void tile_update(SmemMx<T> &S, const MixedStage &st, const Layout &L, int p, int i0,
+                                            int j0, int lane, int warp) {
   constexpr int NT = T::NT;
   const int N = L.N;
-  const MixedStage &st = S.st;
   // Global operands of phase 3 for this thread's four cells, loaded before the
   // barrier so their latency overlaps the wait for the slowest line segment:
   // f s, 1/s, Y0, the accumulator (or the stage input's hp for RK3) and the
@@ -507,24 +508,32 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
   SmemMx<T> &S = *reinterpret_cast<SmemMx<T> *>(smem_f);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-    const WorkItem wi = work[w];
-    {  // stage descriptor into shared memory
-      const int nw = (int)(sizeof(MixedStage) / 4);
-      const int *src = reinterpret_cast<const int *>(stages + wi.inst);
-      int *dst = reinterpret_cast<int *>(&S.st);
-      for (int k = tid; k < nw; k += NT) dst[k] = src[k];
+  constexpr int nwd = (int)(sizeof(MixedStage) / 4);  // descriptor words
+  // the first work item's descriptor; each tile then copies the next one into the
+  // other buffer asynchronously while it computes
+  int buf = 0;
+  if (blockIdx.x < nwork) {
+    const WorkItem wi = work[blockIdx.x];
+    const int *src = reinterpret_cast<const int *>(stages + wi.inst);
+    int *dst = reinterpret_cast<int *>(&S.stb[0]);
+    for (int k = tid; k < nwd; k += NT) dst[k] = src[k];
+    if (tid == 0) S.wib[0] = wi;
+  }
+  __syncthreads();
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x, buf ^= 1) {
+    const MixedStage &st = S.stb[buf];
+    const WorkItem wi = S.wib[buf];
+    const int wn = w + gridDim.x;
+    if (tid == 0 && wn < nwork) S.wib[buf ^ 1] = work[wn];  // read by all after the phase-1 barrier
 #ifdef CCS_BOUNDS
-      // poison the tile arrays: a read of a slot this tile never wrote shows up as
-      // NaN in the result (checked build only)
+    {  // poison the tile arrays (checked build only)
       float *a = S.F;
       const int na = (int)((reinterpret_cast<const char *>(&S.gy[1][T::TY][T::TX - 1]) + sizeof(float) -
                             reinterpret_cast<const char *>(S.F)) / sizeof(float));
       for (int k = tid; k < na; k += NT) a[k] = __int_as_float(0x7fc00000);
-#endif
+      __syncthreads();
     }
-    __syncthreads();
-    const MixedStage &st = S.st;
+#endif
     const Layout L = st.L;
     const int N = L.N, p = wi.panel;
     const int i0 = 1 + wi.tx * TX, j0 = 1 + wi.ty * TY;
@@ -616,17 +625,23 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     }
     __syncthreads();
 
+    if (wn < nwork) {  // the next tile's descriptor, landing during phases 2-4
+      const int *src = reinterpret_cast<const int *>(stages + S.wib[buf ^ 1].inst);
+      int *dst = reinterpret_cast<int *>(&S.stb[buf ^ 1]);
+      for (int k = tid; k < nwd; k += NT) cp_async4(reinterpret_cast<float *>(dst + k),
+                                                      reinterpret_cast<const float *>(src + k));
+    }
     // ---- phase 2: lines -> face values (warps 0-3 rows, 4-7 columns) ---------
     if (!CENTRAL) {  // (the central-difference operators have no faces)
       // segment seg of a line covers faces 0-8 (seg 0) or 8 seg + 1 .. 8 seg + 8
       if (tid < 4 * TY) {
         const int line = tid % TY, seg = tid / TY;
         const int f0 = seg == 0 ? 0 : 1 + 8 * seg, nface = seg == 0 ? 9 : 8;
-        if (j0 + line <= N) tile_line<true, EDISS>(S, S.F, S.uC, st.m.lamx, L, line, f0, nface, i0 - 1, j0 + line);
+        if (j0 + line <= N) tile_line<true, EDISS>(S, st, S.F, S.uC, st.m.lamx, L, line, f0, nface, i0 - 1, j0 + line);
       } else {
         const int t = tid - 4 * TY, line = t % TX, seg = t / TX;
         const int f0 = seg == 0 ? 0 : 1 + 8 * seg, nface = seg == 0 ? 9 : 8;
-        if (i0 + line <= N) tile_line<false, EDISS>(S, S.G, S.vC, st.m.lamy, L, line, f0, nface, j0 - 1, i0 + line);
+        if (i0 + line <= N) tile_line<false, EDISS>(S, st, S.G, S.vC, st.m.lamy, L, line, f0, nface, j0 - 1, i0 + line);
       }
     }
     // phase 3 as an instance per stage kind: the stage kind is the same for every
@@ -634,13 +649,13 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
     // one stage at a time), so the stage update carries no runtime branches and
     // loads only the operands its kind uses
     switch (st.kind) {
-      case K_RK4_1: tile_update<K_RK4_1, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
-      case K_RK4_2: tile_update<K_RK4_2, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
-      case K_RK4_4: tile_update<K_RK4_4, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
-      case K_RK3_1: tile_update<K_RK3_1, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
-      case K_RK3_2: tile_update<K_RK3_2, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
-      case K_RK3_3: tile_update<K_RK3_3, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
-      default: tile_update<K_TEND, T, CENTRAL>(S, L, p, i0, j0, lane, warp); break;
+      case K_RK4_1: tile_update<K_RK4_1, T, CENTRAL>(S, st, L, p, i0, j0, lane, warp); break;
+      case K_RK4_2: tile_update<K_RK4_2, T, CENTRAL>(S, st, L, p, i0, j0, lane, warp); break;
+      case K_RK4_4: tile_update<K_RK4_4, T, CENTRAL>(S, st, L, p, i0, j0, lane, warp); break;
+      case K_RK3_1: tile_update<K_RK3_1, T, CENTRAL>(S, st, L, p, i0, j0, lane, warp); break;
+      case K_RK3_2: tile_update<K_RK3_2, T, CENTRAL>(S, st, L, p, i0, j0, lane, warp); break;
+      case K_RK3_3: tile_update<K_RK3_3, T, CENTRAL>(S, st, L, p, i0, j0, lane, warp); break;
+      default: tile_update<K_TEND, T, CENTRAL>(S, st, L, p, i0, j0, lane, warp); break;
     }
 
     // ---- phase 4: ghost push of the tile's edge strips ----------------------
@@ -682,6 +697,7 @@ mixed_stage_kernel(const MixedStage *__restrict__ stages, const WorkItem *__rest
         st.out.v[d] = (float)vd;
       }
     }
+    cp_async_wait_all();  // this thread's copies of the next descriptor have landed
     __syncthreads();
   }
 }
