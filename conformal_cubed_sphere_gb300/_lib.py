@@ -111,6 +111,7 @@ SIGNATURES = {
     "ccs_timing": (C.c_int, [_vp, C.c_int, C.c_int, _dp, C.POINTER(C.c_int64)]),
     "ccs_stream": (C.c_void_p, [_vp]),
     "ccs_selftest_div": (C.c_int, [_dp, C.c_int64, C.c_double, _dp, _dp]),
+    "ccs_selftest_div_pairs": (C.c_int, [_dp, _dp, C.c_int64, _dp, _dp]),
     "ccs_debug_bounds": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
     "ccs_courant": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ccs_debug_bounds_selftest": (C.c_int, []),

@@ -478,6 +478,29 @@ int ccs_selftest_div(const double *x, int64_t n, double b, double *fast, double 
   return rc;
 }
 
+int ccs_selftest_div_pairs(const double *a, const double *b, int64_t n, double *fast, double *ieee) {
+  if (!a || !b || n <= 0 || !fast || !ieee) return CCS_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CCS_ERR_NODEVICE;
+  cudaSetDevice(0);
+  double *da = nullptr, *dout = nullptr;
+  if (cudaMalloc(&da, 2 * n * sizeof(double)) != cudaSuccess) return CCS_ERR_NOMEM;
+  if (cudaMalloc(&dout, 2 * n * sizeof(double)) != cudaSuccess) {
+    cudaFree(da);
+    return CCS_ERR_NOMEM;
+  }
+  int rc = CCS_OK;
+  if (cudaMemcpy(da, a, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(da + n, b, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      launch_div_pairs_check(da, da + n, n, dout, 0) != cudaSuccess ||
+      cudaMemcpy(fast, dout, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(ieee, dout + n, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = CCS_ERR_CUDA;
+  cudaFree(da);
+  cudaFree(dout);
+  return rc;
+}
+
 const char *ccs_strerror(int status) {
   switch (status) {
     case CCS_OK: return "ok";

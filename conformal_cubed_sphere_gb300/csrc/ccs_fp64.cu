@@ -55,6 +55,17 @@ __device__ __forceinline__ double ccs_div_const(double x, double b, double y) {
   return t - 1ull >= 0xffe0000000000000ull - 1ull ? q0 : q1;
 }
 
+// a / b for a divisor b shared by several quotients, from y = RN(1 / b) computed
+// once: q0 = RN(a y), the exact remainder r = a - q0 b in one FMA, and q0 + r y
+// rounded once, which is RN(a / b) when the quotient is a normal number (Markstein's
+// correction, as in ccs_div_const).  The GPU test suite checks it against IEEE
+// division on random operands.
+__device__ __forceinline__ double ccs_div_by(double a, double b, double y) {
+  const double q0 = a * y;
+  const double r = fma(-q0, b, a);
+  return fma(r, y, q0);
+}
+
 namespace {
 
 // Comparisons of non-negative doubles on the integer pipes: for +0 and positive
@@ -114,7 +125,16 @@ __device__ __forceinline__ double weno5z(double q0, double q1, double q2, double
     const double al1 = 0.6 * (1. + tau5 / (eps + be1));
     const double al2 = 0.3 * (1. + tau5 / (eps + be2));
     const double sum = ((0. + al0) + al1) + al2;
-    w0 = al0 / sum; w1 = al1 / sum; w2 = al2 / sum;
+    // omega = alpha / sum(alpha): one IEEE reciprocal for the three quotients.  Each
+    // alpha is at least its linear weight (0.1) and sum >= alpha, so the quotients lie
+    // in (2^-1004, 1] whenever sum < 2^1000 (tested on the bits); a larger, infinite
+    // or NaN sum takes IEEE division
+    if (__double_as_longlong(sum) < 0x7e70000000000000LL) {
+      const double ys = 1. / sum;
+      w0 = ccs_div_by(al0, sum, ys); w1 = ccs_div_by(al1, sum, ys); w2 = ccs_div_by(al2, sum, ys);
+    } else {
+      w0 = al0 / sum; w1 = al1 / sum; w2 = al2 / sum;
+    }
   }
   return ((0. + s0 * w0) + s1 * w1) + s2 * w2;
 }
@@ -405,6 +425,20 @@ __global__ void div_const_check_kernel(const double *__restrict__ x, int64_t n, 
     out[k] = ccs_div_const(x[k], b, y);
     out[n + k] = x[k] / b;
   }
+}
+
+// test support: out[k] = ccs_div_by(a[k], b[k], 1 / b[k]) next to out[n + k] = a[k] / b[k]
+__global__ void div_pairs_check_kernel(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
+                                       double *__restrict__ out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    out[k] = ccs_div_by(a[k], b[k], 1. / b[k]);
+    out[n + k] = a[k] / b[k];
+  }
+}
+
+cudaError_t launch_div_pairs_check(const double *a, const double *b, int64_t n, double *out, cudaStream_t s) {
+  div_pairs_check_kernel<<<1024, 256, 0, s>>>(a, b, n, out);
+  return cudaGetLastError();
 }
 
 unsigned long long f64_bounds_take() { return bounds_take_tu(); }

@@ -122,6 +122,8 @@ cudaError_t launch_mixed_diag(const Layout &L, StateMixed st, const float *lohp,
 
 // test support: correctly rounded division by a constant, see ccs_fp64.cu
 cudaError_t launch_div_const_check(const double *x, int64_t n, double b, double *out, cudaStream_t s);
+// test support: division by a shared divisor from its reciprocal, see ccs_fp64.cu
+cudaError_t launch_div_pairs_check(const double *a, const double *b, int64_t n, double *out, cudaStream_t s);
 
 // Bounds-checked build (-DCCS_BOUNDS, ccs_bounds.cuh): the first out-of-range index
 // the FP64 / mixed kernels met since the last call, (site << 48) | (index & 2^48-1),

@@ -286,6 +286,14 @@ int ccs_timing(ccs_handle *h, int enable, int reset, double *kernel_ms, int64_t 
  * device 0 with temporary buffers. */
 int ccs_selftest_div(const double *x, int64_t n, double b, double *fast, double *ieee);
 
+/* Self-check of the FP64 lane's division by a divisor several quotients share (the
+ * WENO-Z weights alpha_k / sum(alpha)): for each pair the device computes the
+ * quotient the kernels use, from the divisor's IEEE reciprocal and one FMA
+ * correction (fast[k]), and the IEEE quotient a[k] / b[k] (ieee[k]); they must agree
+ * bit for bit when the quotient is a normal number.  Runs on device 0 with temporary
+ * buffers. */
+int ccs_selftest_div_pairs(const double *a, const double *b, int64_t n, double *fast, double *ieee);
+
 /* Bounds-checked build (libccs_gpu.so built with -DCCS_BOUNDS, build.build_bounds):
  * the kernels check their array indices and skip, instead of performing, any access
  * outside its array, recording the first such index.  ccs_debug_bounds waits for

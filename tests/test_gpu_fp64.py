@@ -172,6 +172,40 @@ def test_constant_division_is_correctly_rounded(b):
     assert np.isnan(fast[10]) and np.isnan(ieee[10])
 
 
+def test_shared_divisor_division_is_correctly_rounded():
+    """The WENO-Z weights alpha_k / sum(alpha) share their divisor: the FP64 lane takes
+    its IEEE reciprocal once and corrects each product with one FMA.  Every quotient
+    must equal IEEE division bit for bit: random significands and exponents (normal
+    quotients), divisors with all-ones and all-zeros significands, and the kernels'
+    own range (0.1 <= a <= b)."""
+    import ctypes as C
+    rng = np.random.default_rng(77)
+    n = 1 << 23
+
+    def doubles(exp_lo, exp_hi, size):
+        sig = rng.integers(0, 1 << 52, size=size, dtype=np.uint64)
+        exp = rng.integers(exp_lo, exp_hi, size=size, dtype=np.uint64)
+        return ((exp << np.uint64(52)) | sig).view(np.float64).copy()
+
+    a = doubles(1023 - 400, 1023 + 400, n)
+    b = doubles(1023 - 400, 1023 + 400, n)
+    q = n // 4  # the kernels' range: a >= 0.1, b = a + (two more such terms)
+    a[:q] = 0.1 + rng.random(q) * rng.choice([1.0, 1e3, 1e9], size=q)
+    b[:q] = a[:q] + (0.7 + rng.random(q) * rng.choice([1.0, 1e3, 1e12], size=q))
+    m = 1 << 16  # divisors whose significand is all ones or all zeros
+    expb = rng.integers(1023 - 300, 1023 + 300, size=m, dtype=np.uint64) << np.uint64(52)
+    b[q:q + m] = (expb | np.uint64((1 << 52) - 1)).view(np.float64)
+    b[q + m:q + 2 * m] = expb.view(np.float64)
+    fast = np.empty(n)
+    ieee = np.empty(n)
+    dp = C.POINTER(C.c_double)
+    rc = L.lib().ccs_selftest_div_pairs(a.ctypes.data_as(dp), b.ctypes.data_as(dp), n, fast.ctypes.data_as(dp),
+                                        ieee.ctypes.data_as(dp))
+    assert rc == 0
+    assert np.array_equal(ieee, a / b)
+    assert np.array_equal(fast.view(np.int64), ieee.view(np.int64))
+
+
 @pytest.mark.parametrize("op", [L.CCS_OP_CENTRAL2, L.CCS_OP_CENTRAL4, L.CCS_OP_CENTRAL6])
 def test_central_difference_operator_bitwise(op):
     """spatial_operators_mod_{2nd,4th,6th}.F90: tendency and 5 RK4 steps bit for bit."""
