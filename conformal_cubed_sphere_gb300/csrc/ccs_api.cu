@@ -345,6 +345,8 @@ static int build_f64_lane(ccs_handle *h) {
   base.accphiG = h->acc[0]; base.accu = h->acc[1]; base.accv = h->acc[2];
   base.dx = c.dx; base.dy = c.dy;
   base.dx60 = 60. * c.dx; base.dy60 = 60. * c.dy;
+  base.rdx = 1. / base.dx; base.rdy = 1. / base.dy;
+  base.rdx60 = 1. / base.dx60; base.rdy60 = 1. / base.dy60;
   base.ediss = c.e_dissipation;
   base.op = h->op;
   auto mk = [&](int kind, int in, int out, double c1) {

@@ -36,8 +36,9 @@ constexpr int NCELL_ARR = 11;
 
 }  // namespace
 
-// x / b for the constant divisors b = 3, 6, 12 of the reference (x/3., x/6.,
-// A*A*13./12.), correctly rounded: q0 = RN(x y) with y = RN(1/b), the remainder
+// x / b for a divisor fixed in advance — the constants 3, 6, 12 of the reference
+// (x/3., x/6., A*A*13./12.) and a grid's dx, dy, 60 dx, 60 dy — correctly rounded:
+// q0 = RN(x y) with y = RN(1/b), the remainder
 // r = x - q0 b is exact in one FMA, and q0 + r y rounded once is RN(x / b)
 // (Markstein's correction, IBM J. Res. Dev. 34(1), 1990) when the quotient does not
 // underflow.  Where the correction does not apply, q0 is already the IEEE result: a
@@ -298,15 +299,19 @@ f64_stage_kernel(const F64Stage *__restrict__ stages, const WorkItem *__restrict
           const double *FF = rec, *EF = rec + NF;
           const int xl = lj * (TX + 1) + li, xr = xl + 1;
           const int yb = NFX + lj * TX + li, yt = yb + TX;
-          dfluxdx = (FF[xr] - FF[xl]) / st.dx;
-          dEdx = (EF[xr] - EF[xl]) / st.dx;
+          // divisions by dx, dy, 60 dx, 60 dy (spatial_operators_mod.F90:153-169) from
+          // their reciprocals, corrected to the IEEE quotients (ccs_div_const)
+          dfluxdx = ccs_div_const(FF[xr] - FF[xl], st.dx, st.rdx);
+          dEdx = ccs_div_const(EF[xr] - EF[xl], st.dx, st.rdx);
           const double *vr = S.v + (lj + 3) * RX + li;  // v(i-3 .. i+3) at vr[0..6]
-          dvdx = (-vr[0] + 9. * vr[1] - 45. * vr[2] + 45. * vr[4] - 9. * vr[5] + vr[6]) / st.dx60;
-          dfluxdy = (FF[yt] - FF[yb]) / st.dy;
-          dEdy = (EF[yt] - EF[yb]) / st.dy;
+          dvdx = ccs_div_const(-vr[0] + 9. * vr[1] - 45. * vr[2] + 45. * vr[4] - 9. * vr[5] + vr[6], st.dx60,
+                               st.rdx60);
+          dfluxdy = ccs_div_const(FF[yt] - FF[yb], st.dy, st.rdy);
+          dEdy = ccs_div_const(EF[yt] - EF[yb], st.dy, st.rdy);
           const double *uc = S.u + lj * RX + li + 3;  // u(j-3 .. j+3) at uc[k * RX]
-          dudy = (-uc[0] + 9. * uc[RX] - 45. * uc[2 * RX] + 45. * uc[4 * RX] - 9. * uc[5 * RX] + uc[6 * RX]) /
-                 st.dy60;
+          dudy = ccs_div_const(-uc[0] + 9. * uc[RX] - 45. * uc[2 * RX] + 45. * uc[4 * RX] - 9. * uc[5 * RX] +
+                                   uc[6 * RX],
+                               st.dy60, st.rdy60);
         } else {
           dfluxdx = central_diff(op, S.Fx + rc, 1, st.dx);
           dEdx = central_diff(op, S.E + rc, 1, st.dx);

@@ -54,6 +54,7 @@ struct F64Stage {
   double *zonal, *merid;  // sphere winds of Y_{k+1} when non-null
   double *tphiG, *tu, *tv;
   double dx, dy, dx60, dy60, c1;
+  double rdx, rdy, rdx60, rdy60;  // RN(1 / dx) etc.: the divisions by them are corrected to IEEE
   int kind, ediss;
   int op;  // CCS_OP_WENO, or the central-difference order 2 / 4 / 6
 };
