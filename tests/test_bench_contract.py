@@ -72,3 +72,23 @@ def test_fp64_roofline():
     assert r["peak"] == pytest.approx(2 * 152 * 2070e6)
     assert r["frac"] == pytest.approx(1.9e9 / 3.5e-3 / (2 * 152 * 2070e6))
     assert bench.fp64_roofline(3.5, None, 152, {"sm_mhz": 2070.0}) is None
+
+
+def test_counters_cover_both_32_wide_mixed_tiles():
+    """The autotuner picks either 32-wide mixed tile at C384 (they run within a few
+    tenths of a percent of each other), so the committed counters hold both."""
+    d = json.loads((ROOT / "profiles" / "roofline_traffic.json").read_text())
+    for v in ("0", "1"):
+        c = d["mixed_C384"][v]
+        assert c["dram_bytes"] > 0 and c["warp_inst"] > 0
+        assert len(c["dram_bytes_per_launch"]) == len(c["warp_inst_per_launch"]) == 4
+    assert d["f64_stage_C384_fp64_thread_inst"] > 0
+
+
+def test_variant_names():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from conformal_cubed_sphere_gb300 import _lib as L
+    assert [bench.variant_name("mixed", v) for v in range(len(L.MIXED_VARIANTS))] == \
+        ["32x32 loads", "32x16 loads", "32x32 async", "32x16 async"]
+    assert [bench.variant_name("fp64", v) for v in range(3)] == ["32x8", "16x16", "64x4"]
